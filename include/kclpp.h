@@ -1,0 +1,230 @@
+/*
+ * kclpp.h -- C ABI of the GB300 KClist++ library (libkclpp.so).
+ *
+ * The reference (btsun/kclistpp) is a set of stand-alone C programs with no
+ * library interface; these entry points replace the C functions those programs
+ * call, keeping their meaning, and add the status codes, explicit buffers and
+ * device residency the reference lacks.  Every declaration cites the reference
+ * function it replaces (file:line in the reference tree).
+ *
+ * Conventions
+ *  - Every call returns kclpp_status (0 = KCLPP_OK).  kclpp_last_error() gives a
+ *    thread-local message for the last failure.  No exception crosses the ABI.
+ *  - Host buffers are caller-owned.  Device buffers (the *_dev entry points)
+ *    are caller-owned device pointers on the context's device.  Handles
+ *    (kclpp_ctx, kclpp_edge_list, kclpp_graph, kclpp_trim_result) are owned by
+ *    the library and released with their *_free / kclpp_destroy call.
+ *  - A context owns one CUDA stream (the caller's, if one is given) and is
+ *    meant for one host thread at a time.
+ *  - Graphs must be simple: no self loops and no repeated edges (the
+ *    reference reads such input but counts cliques with multiplicity).
+ *  - Vertex ids are uint32; CSR offsets are uint64.  After orientation an edge
+ *    is s -> t with s > t and out-lists are ascending (Graph.c:95-156).
+ */
+#ifndef KCLPP_H_
+#define KCLPP_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ---------------------------------------------------------- */
+typedef int kclpp_status;
+#define KCLPP_OK 0
+#define KCLPP_ERR_INVALID 1     /* bad argument, or input graph not simple      */
+#define KCLPP_ERR_IO 2          /* file cannot be opened / written              */
+#define KCLPP_ERR_NOMEM 3       /* host or device allocation failed             */
+#define KCLPP_ERR_CUDA 4        /* CUDA runtime error                           */
+#define KCLPP_ERR_UNSUPPORTED 5 /* k or out-degree beyond the compiled limits   */
+#define KCLPP_ERR_OVERFLOW 6    /* a device counter would have wrapped          */
+#define KCLPP_ERR_NODEVICE 7    /* no CUDA device                               */
+
+#define KCLPP_MAX_K 8           /* largest clique size compiled in              */
+#define KCLPP_MAX_OUTDEG 2048   /* largest out-degree a root may have           */
+
+const char *kclpp_status_string(kclpp_status s);
+const char *kclpp_last_error(void);
+const char *kclpp_version(void);
+
+/* ---- context ---------------------------------------------------------- */
+typedef struct kclpp_ctx kclpp_ctx;
+/* stream: a cudaStream_t to run on, or NULL for a stream the context creates. */
+kclpp_status kclpp_create(int device, void *stream, kclpp_ctx **ctx);
+kclpp_status kclpp_destroy(kclpp_ctx *ctx);
+kclpp_status kclpp_synchronize(kclpp_ctx *ctx);
+/* Number of kernels this context has launched since creation. */
+uint64_t kclpp_launch_count(const kclpp_ctx *ctx);
+
+/* ---- edge lists (A1) --------------------------------------------------- */
+typedef struct kclpp_edge_list kclpp_edge_list;
+/* ReadEdgeList, Graph.c:34-53: "u v" per line, n = max id + 1. */
+kclpp_status kclpp_read_edge_list(const char *path, kclpp_edge_list **out);
+/* pairs = s0 t0 s1 t1 ... (2*e entries); n = max id + 1 as in ReadEdgeList. */
+kclpp_status kclpp_edge_list_create(const uint32_t *pairs, uint64_t e, kclpp_edge_list **out);
+kclpp_status kclpp_edge_list_info(const kclpp_edge_list *el, uint32_t *n, uint64_t *e);
+kclpp_status kclpp_edge_list_copy(const kclpp_edge_list *el, uint32_t *pairs_out);
+kclpp_status kclpp_write_edge_list(const kclpp_edge_list *el, const char *path);
+void kclpp_edge_list_free(kclpp_edge_list *el);
+
+/* Seeded synthetic inputs (no reference counterpart: the paper's datasets are
+ * not distributed).  Undirected, deduplicated, no self loops, sorted (u < v). */
+#define KCLPP_GEN_CHUNG_LU 1
+#define KCLPP_GEN_RMAT 2
+#define KCLPP_GEN_ER 3
+#define KCLPP_GEN_PLANTED 4     /* Chung-Lu base plus planted G(n_c, p) communities */
+typedef struct {
+  int kind;
+  uint32_t n;                   /* vertices (CHUNG_LU, ER, PLANTED)             */
+  double avg_degree;            /* CHUNG_LU, ER, PLANTED                        */
+  double gamma;                 /* power-law exponent (CHUNG_LU, PLANTED)       */
+  uint32_t scale;               /* RMAT: n = 2^scale                            */
+  uint32_t edge_factor;         /* RMAT: samples = edge_factor * n              */
+  double a, b, c;               /* RMAT quadrant probabilities (d = 1-a-b-c)    */
+  uint32_t communities;         /* PLANTED                                      */
+  uint32_t comm_min, comm_max;  /* PLANTED: sizes log-uniform in [min, max]     */
+  double p_in;                  /* PLANTED: edge probability inside             */
+  uint64_t seed;
+} kclpp_gen_params;
+kclpp_status kclpp_generate(const kclpp_gen_params *p, kclpp_edge_list **out);
+
+/* ---- degeneracy order and DAG (A2-A4) ---------------------------------- */
+typedef struct kclpp_graph kclpp_graph;
+/* SortByCore, Graph.c:57-91 (same binary-heap tie order, BinaryHeap.c:6-90):
+ * rank[v] = n - 1 - (pop index of v).  rank_out has n entries. */
+kclpp_status kclpp_core_order(const kclpp_edge_list *el, uint32_t *rank_out);
+/* Relabel + MakeGraph, Graph.c:95-156: orient by rank, sort, out-CSR, upload. */
+kclpp_status kclpp_make_graph(kclpp_ctx *ctx, const kclpp_edge_list *el, const uint32_t *rank,
+                              kclpp_graph **g);
+/* kclpp_core_order followed by kclpp_make_graph (main, kCDensestNoAtom.c:425-427). */
+kclpp_status kclpp_build_graph(kclpp_ctx *ctx, const kclpp_edge_list *el, kclpp_graph **g);
+/* A DAG given directly as host CSR (out-lists strictly below the source and
+ * ascending), e.g. one made by another tool from the same edge list. */
+kclpp_status kclpp_graph_from_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const uint64_t *offsets,
+                                  const uint32_t *cols, kclpp_graph **g);
+/* n, m and core (max out-degree; "Core value" printed at Graph.c:137). */
+kclpp_status kclpp_graph_info(const kclpp_graph *g, uint32_t *n, uint64_t *m, uint32_t *core);
+kclpp_status kclpp_graph_copy_csr(const kclpp_graph *g, uint64_t *offsets, uint32_t *cols);
+void kclpp_graph_free(kclpp_graph *g);
+/* CountEdges, Graph.c:158-166: edges with both ends among nodes[0..num). */
+kclpp_status kclpp_count_edges(kclpp_ctx *ctx, const kclpp_graph *g, uint32_t num_nodes,
+                               const uint32_t *nodes, uint32_t *m_out);
+
+/* ---- k-clique counts (A16 on the DAG) ----------------------------------- */
+/* Number of k-cliques and, if per_vertex != NULL, the k-clique degree of every
+ * vertex (onepass/recursion, kClistCoreTrim.c:368-416). */
+kclpp_status kclpp_count_cliques(kclpp_ctx *ctx, const kclpp_graph *g, int k,
+                                 uint64_t *per_vertex, uint64_t *total);
+
+/* ---- Seq-kClist++ (A7) --------------------------------------------------- */
+/* Deterministic pass orderings.  EDGE_STREAMS: every root edge runs the
+ * reference's in-place "++" chain (kCDensestNoAtom.c:155-268) from the
+ * pass-start r, and the per-edge increments are summed -- the reference's
+ * CDF_CliqueEnum (kCDensestNoAtom.c:270-295) with one thread per root edge. */
+#define KCLPP_SEQ_EDGE_STREAMS 1
+/* `passes` FRANK_WOLFE passes (CDF_CliqueEnum, kCDensestNoAtom.c:270-295) on
+ * r (n entries, u64 as in kCDensestNoAtom.c:124). */
+kclpp_status kclpp_seq_passes(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t passes,
+                              int det_mode, uint64_t *r_inout);
+kclpp_status kclpp_seq_passes_dev(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t passes,
+                                  int det_mode, uint64_t *r_inout_dev);
+/* One-shot call for callers that hold only a host CSR: uploads the DAG, runs
+ * `passes` passes on host r, and downloads r (the reference's data stays on
+ * the host in the same way). */
+kclpp_status kclpp_seq_passes_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const uint64_t *offsets,
+                                  const uint32_t *cols, int k, uint32_t passes, int det_mode,
+                                  uint64_t *r_inout);
+
+/* ---- Sim-kClist++ (A8, A9) ------------------------------------------------ */
+/* rho_add of one FRANK_WOLFE pass (kCDensestCmpSync.c:138-146, 298-325): cnt[v]
+ * = number of k-cliques whose (rho, id)-smallest member is v. */
+kclpp_status kclpp_sim_counts(kclpp_ctx *ctx, const kclpp_graph *g, int k, const double *rho,
+                              uint64_t *cnt);
+/* Passes t_first .. t_first+passes-1 of CDF_Main's loop (kCDensestCmpSync.c:396-404):
+ * rho = (t*rho + 2*rho_add) / (t + 2), IEEE double, no fused multiply-add. */
+kclpp_status kclpp_sim_passes(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t t_first,
+                              uint32_t passes, double *rho_inout);
+kclpp_status kclpp_sim_passes_dev(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t t_first,
+                                  uint32_t passes, double *rho_inout_dev);
+kclpp_status kclpp_sim_passes_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const uint64_t *offsets,
+                                  const uint32_t *cols, int k, uint32_t t_first, uint32_t passes,
+                                  double *rho_inout);
+
+/* ---- sort by r, PAVA pass, densest prefix (A10-A13) ------------------------ */
+/* CDF_NodeCmp + qsort (kCDensestNoAtom.c:322-337): vertices by r descending,
+ * ties by ascending id; level[reordered[i]] = i.  Either output may be NULL. */
+kclpp_status kclpp_sort_by_r_u64(kclpp_ctx *ctx, uint32_t n, const uint64_t *r, uint32_t *reordered,
+                                 uint32_t *level);
+/* Sim's key truncates r to unsigned long long first (kCDensestCmpSync.c:334-340). */
+kclpp_status kclpp_sort_by_r_f64(kclpp_ctx *ctx, uint32_t n, const double *r, uint32_t *reordered,
+                                 uint32_t *level);
+/* PAVA_PREPROCESS pass (kCDensestNoAtom.c:191-213, 296-309): tentative[i] =
+ * cliques whose largest-level member has level i. */
+kclpp_status kclpp_pava(kclpp_ctx *ctx, const kclpp_graph *g, int k, const uint32_t *level,
+                        uint64_t *tentative);
+typedef struct {
+  uint32_t n;        /* vertices in the densest prefix                    */
+  uint32_t m;        /* edges among them (CountEdges)                     */
+  uint64_t cliques;  /* k-cliques among them: density = cliques / n       */
+  double density;
+  double ub;         /* upper bound on the maximum k-clique density       */
+} kclpp_densest_info;
+/* CDF_FindDensestSubset, kCDensestNoAtom.c:330-371 (T = passes behind r). */
+kclpp_status kclpp_extract_densest_seq(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t T,
+                                       const uint64_t *r, kclpp_densest_info *info,
+                                       uint32_t *reordered_out);
+/* CDF_FindDensestSubset, kCDensestCmpSync.c:342-383. */
+kclpp_status kclpp_extract_densest_sim(kclpp_ctx *ctx, const kclpp_graph *g, int k,
+                                       const double *rho, kclpp_densest_info *info,
+                                       uint32_t *reordered_out);
+
+/* ---- whole runs (A14) ------------------------------------------------------ */
+/* CDF_Main (kCDensestNoAtom.c:373-402): passes 1..2^floor(log2 num_iter), one
+ * info per power of two (at most max_infos stored; *n_infos = number made). */
+kclpp_status kclpp_seq_main(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t num_iter,
+                            int det_mode, uint64_t *r_out, kclpp_densest_info *infos,
+                            int max_infos, int *n_infos);
+/* CDF_Main (kCDensestCmpSync.c:385-419). */
+kclpp_status kclpp_sim_main(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t num_iter,
+                            double *rho_out, kclpp_densest_info *infos, int max_infos,
+                            int *n_infos);
+
+/* ---- k-clique core trim (A15-A18) ------------------------------------------ */
+#define KCLPP_TRIM_EXACT 0  /* the reference's heap peel: core numbers, peel order,
+                               best suffix and trimmed set identical to it */
+#define KCLPP_TRIM_FAST 1   /* GPU density-threshold trimming: the rho-core for the
+                               best density seen; no core numbers */
+typedef struct kclpp_trim_result kclpp_trim_result;
+typedef struct {
+  uint32_t n, n2;        /* input vertices; vertices with core >= k-1          */
+  uint64_t e, e2;        /* input edges; edges among the n2                    */
+  uint32_t core;         /* degeneracy of the input                            */
+  uint64_t total;        /* k-cliques in the graph                             */
+  uint64_t ckcore;       /* k-clique core number of the graph (EXACT)          */
+  double ckrho;          /* best k-clique density found along the peel         */
+  double rho;            /* its edge density                                   */
+  uint32_t size;         /* its size                                           */
+  uint32_t ntrim;        /* vertices kept                                      */
+  uint64_t mtrim;        /* edges kept                                         */
+  uint64_t ncktrim;      /* k-cliques kept                                     */
+} kclpp_trim_info;
+/* main of kClistCoreTrim.c:707-775: kcore (:242-272), relabelnodes (:274-294),
+ * mkspecial (:306-331), onepass (:394-416), kcliquecore (:605-666). */
+kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int k, int mode,
+                        kclpp_trim_result **out);
+kclpp_status kclpp_trim_info_get(const kclpp_trim_result *t, kclpp_trim_info *info);
+/* Per surviving vertex (new labels 0..n2-1): original id (map), k-clique degree
+ * (the ckdeg file, :419-429), and along the peel order: vertex and core number
+ * (the ckcore file, :672-676).  Any output may be NULL. */
+kclpp_status kclpp_trim_copy(const kclpp_trim_result *t, uint32_t *map, uint64_t *nck,
+                             uint32_t *order, uint64_t *core_num);
+/* The trimmed graph in original ids and input order (printdensest, :686-699). */
+kclpp_status kclpp_trim_edges(const kclpp_trim_result *t, kclpp_edge_list **out);
+void kclpp_trim_free(kclpp_trim_result *t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

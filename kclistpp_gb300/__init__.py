@@ -1,0 +1,463 @@
+"""GB300-native KClist++: k-clique listing fused with the "++" updates.
+
+Python binding of the C ABI in include/kclpp.h (libkclpp.so, built in-tree by
+kclistpp_gb300.build).  The functions mirror the reference programs' C
+functions (btsun/kclistpp):
+
+    read_edge_list      ReadEdgeList            Graph.c:34-53
+    core_order          SortByCore              Graph.c:57-91
+    build_graph         SortByCore+Relabel+MakeGraph  Graph.c:57-156
+    count_cliques       onepass (k-clique degrees)    kClistCoreTrim.c:394-416
+    seq_passes          CDF_CliqueEnum(FRANK_WOLFE)   kCDensestNoAtom.c:270-295
+    sim_counts          CDF_CliqueEnum(FRANK_WOLFE)   kCDensestCmpSync.c:298-325
+    sim_passes          + rho update                  kCDensestCmpSync.c:396-404
+    sort_by_r_*         CDF_NodeCmp + qsort           kCDensestNoAtom.c:322-337
+    pava                CDF_CliqueEnum(PAVA_PREPROCESS) kCDensestNoAtom.c:296-309
+    extract_densest_*   CDF_FindDensestSubset         kCDensestNoAtom.c:330-371
+    seq_main/sim_main   CDF_Main                      kCDensestNoAtom.c:373-402
+    trim                kClistCoreTrim main           kClistCoreTrim.c:707-775
+
+Every call runs through the CUDA library; there is no CPU fallback.  If the
+library has not been built (or cannot be loaded) the import fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libkclpp.so")
+
+OK = 0
+ERR_INVALID, ERR_IO, ERR_NOMEM, ERR_CUDA, ERR_UNSUPPORTED, ERR_OVERFLOW, ERR_NODEVICE = 1, 2, 3, 4, 5, 6, 7
+MAX_K = 8
+SEQ_EDGE_STREAMS = 1
+TRIM_EXACT, TRIM_FAST = 0, 1
+GEN_CHUNG_LU, GEN_RMAT, GEN_ER, GEN_PLANTED = 1, 2, 3, 4
+
+
+class KclppError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"kclpp status {status}: {msg}")
+        self.status = status
+
+
+class DensestInfo(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("m", C.c_uint32), ("cliques", C.c_uint64),
+                ("density", C.c_double), ("ub", C.c_double)]
+
+    def as_tuple(self):
+        return (self.n, self.m, self.cliques, self.density, self.ub)
+
+    def __repr__(self):
+        return (f"DensestInfo(n={self.n}, m={self.m}, cliques={self.cliques}, "
+                f"density={self.density!r}, ub={self.ub!r})")
+
+
+class TrimInfo(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("n2", C.c_uint32), ("e", C.c_uint64), ("e2", C.c_uint64),
+                ("core", C.c_uint32), ("total", C.c_uint64), ("ckcore", C.c_uint64),
+                ("ckrho", C.c_double), ("rho", C.c_double), ("size", C.c_uint32),
+                ("ntrim", C.c_uint32), ("mtrim", C.c_uint64), ("ncktrim", C.c_uint64)]
+
+
+class GenParams(C.Structure):
+    _fields_ = [("kind", C.c_int), ("n", C.c_uint32), ("avg_degree", C.c_double),
+                ("gamma", C.c_double), ("scale", C.c_uint32), ("edge_factor", C.c_uint32),
+                ("a", C.c_double), ("b", C.c_double), ("c", C.c_double),
+                ("communities", C.c_uint32), ("comm_min", C.c_uint32), ("comm_max", C.c_uint32),
+                ("p_in", C.c_double), ("seed", C.c_uint64)]
+
+
+def _load() -> C.CDLL:
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m kclistpp_gb300.build`")
+    return C.CDLL(LIB_PATH)
+
+
+_lib = _load()
+
+_P = C.c_void_p
+_u32p = C.POINTER(C.c_uint32)
+_u64p = C.POINTER(C.c_uint64)
+_f64p = C.POINTER(C.c_double)
+
+_SIGS = {
+    "kclpp_status_string": (C.c_char_p, [C.c_int]),
+    "kclpp_last_error": (C.c_char_p, []),
+    "kclpp_version": (C.c_char_p, []),
+    "kclpp_create": (C.c_int, [C.c_int, _P, C.POINTER(_P)]),
+    "kclpp_destroy": (C.c_int, [_P]),
+    "kclpp_synchronize": (C.c_int, [_P]),
+    "kclpp_launch_count": (C.c_uint64, [_P]),
+    "kclpp_read_edge_list": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "kclpp_edge_list_create": (C.c_int, [_u32p, C.c_uint64, C.POINTER(_P)]),
+    "kclpp_edge_list_info": (C.c_int, [_P, _u32p, _u64p]),
+    "kclpp_edge_list_copy": (C.c_int, [_P, _u32p]),
+    "kclpp_write_edge_list": (C.c_int, [_P, C.c_char_p]),
+    "kclpp_edge_list_free": (None, [_P]),
+    "kclpp_generate": (C.c_int, [C.POINTER(GenParams), C.POINTER(_P)]),
+    "kclpp_core_order": (C.c_int, [_P, _u32p]),
+    "kclpp_make_graph": (C.c_int, [_P, _P, _u32p, C.POINTER(_P)]),
+    "kclpp_build_graph": (C.c_int, [_P, _P, C.POINTER(_P)]),
+    "kclpp_graph_from_csr": (C.c_int, [_P, C.c_uint32, C.c_uint64, _u64p, _u32p, C.POINTER(_P)]),
+    "kclpp_graph_info": (C.c_int, [_P, _u32p, _u64p, _u32p]),
+    "kclpp_graph_copy_csr": (C.c_int, [_P, _u64p, _u32p]),
+    "kclpp_graph_free": (None, [_P]),
+    "kclpp_count_edges": (C.c_int, [_P, _P, C.c_uint32, _u32p, _u32p]),
+    "kclpp_count_cliques": (C.c_int, [_P, _P, C.c_int, _u64p, _u64p]),
+    "kclpp_seq_passes": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _u64p]),
+    "kclpp_seq_passes_dev": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _P]),
+    "kclpp_seq_passes_csr": (C.c_int, [_P, C.c_uint32, C.c_uint64, _u64p, _u32p, C.c_int, C.c_uint32,
+                                       C.c_int, _u64p]),
+    "kclpp_sim_counts": (C.c_int, [_P, _P, C.c_int, _f64p, _u64p]),
+    "kclpp_sim_passes": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_uint32, _f64p]),
+    "kclpp_sim_passes_dev": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_uint32, _P]),
+    "kclpp_sim_passes_csr": (C.c_int, [_P, C.c_uint32, C.c_uint64, _u64p, _u32p, C.c_int, C.c_uint32,
+                                       C.c_uint32, _f64p]),
+    "kclpp_sort_by_r_u64": (C.c_int, [_P, C.c_uint32, _u64p, _u32p, _u32p]),
+    "kclpp_sort_by_r_f64": (C.c_int, [_P, C.c_uint32, _f64p, _u32p, _u32p]),
+    "kclpp_pava": (C.c_int, [_P, _P, C.c_int, _u32p, _u64p]),
+    "kclpp_extract_densest_seq": (C.c_int, [_P, _P, C.c_int, C.c_uint32, _u64p, C.POINTER(DensestInfo), _u32p]),
+    "kclpp_extract_densest_sim": (C.c_int, [_P, _P, C.c_int, _f64p, C.POINTER(DensestInfo), _u32p]),
+    "kclpp_seq_main": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _u64p, C.POINTER(DensestInfo),
+                                 C.c_int, C.POINTER(C.c_int)]),
+    "kclpp_sim_main": (C.c_int, [_P, _P, C.c_int, C.c_uint32, _f64p, C.POINTER(DensestInfo), C.c_int,
+                                 C.POINTER(C.c_int)]),
+    "kclpp_trim": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(_P)]),
+    "kclpp_trim_info_get": (C.c_int, [_P, C.POINTER(TrimInfo)]),
+    "kclpp_trim_copy": (C.c_int, [_P, _u32p, _u64p, _u32p, _u64p]),
+    "kclpp_trim_edges": (C.c_int, [_P, C.POINTER(_P)]),
+    "kclpp_trim_free": (None, [_P]),
+}
+for _name, (_res, _args) in _SIGS.items():
+    _f = getattr(_lib, _name)
+    _f.restype = _res
+    _f.argtypes = _args
+
+#: Every function the header declares (checked by the tests).
+EXPORTED = tuple(_SIGS)
+
+
+def _check(status: int) -> None:
+    if status != OK:
+        raise KclppError(status, _lib.kclpp_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def version() -> str:
+    return _lib.kclpp_version().decode()
+
+
+class Context:
+    """One device and one CUDA stream (the caller's, if `stream` is given)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        h = _P()
+        _check(_lib.kclpp_create(device, _P(stream) if stream else None, C.byref(h)))
+        self._h = h
+
+    @property
+    def handle(self):
+        return self._h
+
+    def synchronize(self) -> None:
+        _check(_lib.kclpp_synchronize(self._h))
+
+    def launches(self) -> int:
+        return int(_lib.kclpp_launch_count(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.kclpp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class EdgeList:
+    """Host edge list; n = max id + 1 as ReadEdgeList computes it."""
+
+    def __init__(self, handle):
+        self._h = handle
+
+    @classmethod
+    def from_pairs(cls, pairs) -> "EdgeList":
+        a = np.ascontiguousarray(np.asarray(pairs, dtype=np.uint32).reshape(-1, 2))
+        h = _P()
+        _check(_lib.kclpp_edge_list_create(_ptr(a, C.c_uint32), a.shape[0], C.byref(h)))
+        return cls(h)
+
+    def info(self) -> tuple[int, int]:
+        n, e = C.c_uint32(), C.c_uint64()
+        _check(_lib.kclpp_edge_list_info(self._h, C.byref(n), C.byref(e)))
+        return n.value, e.value
+
+    @property
+    def n(self) -> int:
+        return self.info()[0]
+
+    @property
+    def e(self) -> int:
+        return self.info()[1]
+
+    def pairs(self) -> np.ndarray:
+        n, e = self.info()
+        out = np.empty((e, 2), dtype=np.uint32)
+        if e:
+            _check(_lib.kclpp_edge_list_copy(self._h, _ptr(out, C.c_uint32)))
+        return out
+
+    def write(self, path: str) -> None:
+        _check(_lib.kclpp_write_edge_list(self._h, os.fsencode(path)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.kclpp_edge_list_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def read_edge_list(path: str) -> EdgeList:
+    h = _P()
+    _check(_lib.kclpp_read_edge_list(os.fsencode(path), C.byref(h)))
+    return EdgeList(h)
+
+
+def generate(kind: int, *, n=0, avg_degree=0.0, gamma=0.0, scale=0, edge_factor=0, a=0.0, b=0.0, c=0.0,
+             communities=0, comm_min=0, comm_max=0, p_in=0.0, seed=1) -> EdgeList:
+    p = GenParams(kind, n, avg_degree, gamma, scale, edge_factor, a, b, c, communities, comm_min,
+                  comm_max, p_in, seed)
+    h = _P()
+    _check(_lib.kclpp_generate(C.byref(p), C.byref(h)))
+    return EdgeList(h)
+
+
+def chung_lu(n: int, avg_degree: float, gamma: float, seed: int = 1) -> EdgeList:
+    return generate(GEN_CHUNG_LU, n=n, avg_degree=avg_degree, gamma=gamma, seed=seed)
+
+
+def rmat(scale: int, edge_factor: int = 16, a=0.57, b=0.19, c=0.19, seed: int = 1) -> EdgeList:
+    return generate(GEN_RMAT, scale=scale, edge_factor=edge_factor, a=a, b=b, c=c, seed=seed)
+
+
+def erdos_renyi(n: int, avg_degree: float, seed: int = 1) -> EdgeList:
+    return generate(GEN_ER, n=n, avg_degree=avg_degree, seed=seed)
+
+
+def planted(n: int, avg_degree: float, gamma: float, communities: int, comm_min: int, comm_max: int,
+            p_in: float, seed: int = 1) -> EdgeList:
+    return generate(GEN_PLANTED, n=n, avg_degree=avg_degree, gamma=gamma, communities=communities,
+                    comm_min=comm_min, comm_max=comm_max, p_in=p_in, seed=seed)
+
+
+def core_order(el: EdgeList) -> np.ndarray:
+    rank = np.empty(el.n, dtype=np.uint32)
+    _check(_lib.kclpp_core_order(el._h, _ptr(rank, C.c_uint32)))
+    return rank
+
+
+class Graph:
+    """Degeneracy-oriented DAG resident on the device."""
+
+    def __init__(self, ctx: Context, handle):
+        self.ctx = ctx
+        self._h = handle
+        n, m, core = C.c_uint32(), C.c_uint64(), C.c_uint32()
+        _check(_lib.kclpp_graph_info(handle, C.byref(n), C.byref(m), C.byref(core)))
+        self.n, self.m, self.core = n.value, m.value, core.value
+
+    def csr(self) -> tuple[np.ndarray, np.ndarray]:
+        off = np.empty(self.n + 1, dtype=np.uint64)
+        cols = np.empty(self.m, dtype=np.uint32)
+        _check(_lib.kclpp_graph_copy_csr(self._h, _ptr(off, C.c_uint64), _ptr(cols, C.c_uint32)))
+        return off, cols
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.kclpp_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def build_graph(ctx: Context, el: EdgeList, rank: np.ndarray | None = None) -> Graph:
+    h = _P()
+    if rank is None:
+        _check(_lib.kclpp_build_graph(ctx.handle, el._h, C.byref(h)))
+    else:
+        rank = np.ascontiguousarray(rank, dtype=np.uint32)
+        _check(_lib.kclpp_make_graph(ctx.handle, el._h, _ptr(rank, C.c_uint32), C.byref(h)))
+    return Graph(ctx, h)
+
+
+def graph_from_csr(ctx: Context, offsets: np.ndarray, cols: np.ndarray) -> Graph:
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    cl = np.ascontiguousarray(cols, dtype=np.uint32)
+    h = _P()
+    _check(_lib.kclpp_graph_from_csr(ctx.handle, len(off) - 1, len(cl), _ptr(off, C.c_uint64),
+                                     _ptr(cl, C.c_uint32), C.byref(h)))
+    return Graph(ctx, h)
+
+
+def count_edges(g: Graph, nodes: np.ndarray) -> int:
+    nodes = np.ascontiguousarray(nodes, dtype=np.uint32)
+    m = C.c_uint32()
+    _check(_lib.kclpp_count_edges(g.ctx.handle, g._h, len(nodes), _ptr(nodes, C.c_uint32), C.byref(m)))
+    return m.value
+
+
+def count_cliques(g: Graph, k: int) -> tuple[int, np.ndarray]:
+    per = np.empty(g.n, dtype=np.uint64)
+    tot = C.c_uint64()
+    _check(_lib.kclpp_count_cliques(g.ctx.handle, g._h, k, _ptr(per, C.c_uint64), C.byref(tot)))
+    return tot.value, per
+
+
+def seq_passes(g: Graph, k: int, passes: int, r: np.ndarray | None = None,
+               det_mode: int = SEQ_EDGE_STREAMS) -> np.ndarray:
+    r = np.zeros(g.n, dtype=np.uint64) if r is None else np.array(r, dtype=np.uint64, copy=True)
+    _check(_lib.kclpp_seq_passes(g.ctx.handle, g._h, k, passes, det_mode, _ptr(r, C.c_uint64)))
+    return r
+
+
+def seq_passes_csr(ctx: Context, offsets, cols, k: int, passes: int, r: np.ndarray,
+                   det_mode: int = SEQ_EDGE_STREAMS) -> None:
+    """One-shot host call (upload DAG + passes + download); r is updated in place."""
+    _check(_lib.kclpp_seq_passes_csr(ctx.handle, len(offsets) - 1, len(cols), _ptr(offsets, C.c_uint64),
+                                     _ptr(cols, C.c_uint32), k, passes, det_mode, _ptr(r, C.c_uint64)))
+
+
+def sim_counts(g: Graph, k: int, rho: np.ndarray) -> np.ndarray:
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    cnt = np.empty(g.n, dtype=np.uint64)
+    _check(_lib.kclpp_sim_counts(g.ctx.handle, g._h, k, _ptr(rho, C.c_double), _ptr(cnt, C.c_uint64)))
+    return cnt
+
+
+def sim_passes(g: Graph, k: int, passes: int, rho: np.ndarray | None = None, t_first: int = 1) -> np.ndarray:
+    rho = np.zeros(g.n, dtype=np.float64) if rho is None else np.array(rho, dtype=np.float64, copy=True)
+    _check(_lib.kclpp_sim_passes(g.ctx.handle, g._h, k, t_first, passes, _ptr(rho, C.c_double)))
+    return rho
+
+
+def sim_passes_csr(ctx: Context, offsets, cols, k: int, passes: int, rho: np.ndarray, t_first: int = 1) -> None:
+    _check(_lib.kclpp_sim_passes_csr(ctx.handle, len(offsets) - 1, len(cols), _ptr(offsets, C.c_uint64),
+                                     _ptr(cols, C.c_uint32), k, t_first, passes, _ptr(rho, C.c_double)))
+
+
+def sort_by_r_u64(r: np.ndarray, ctx: Context | None = None) -> tuple[np.ndarray, np.ndarray]:
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    n = len(r)
+    re, lv = np.empty(n, dtype=np.uint32), np.empty(n, dtype=np.uint32)
+    _check(_lib.kclpp_sort_by_r_u64(ctx.handle if ctx else None, n, _ptr(r, C.c_uint64),
+                                    _ptr(re, C.c_uint32), _ptr(lv, C.c_uint32)))
+    return re, lv
+
+
+def sort_by_r_f64(r: np.ndarray, ctx: Context | None = None) -> tuple[np.ndarray, np.ndarray]:
+    r = np.ascontiguousarray(r, dtype=np.float64)
+    n = len(r)
+    re, lv = np.empty(n, dtype=np.uint32), np.empty(n, dtype=np.uint32)
+    _check(_lib.kclpp_sort_by_r_f64(ctx.handle if ctx else None, n, _ptr(r, C.c_double),
+                                    _ptr(re, C.c_uint32), _ptr(lv, C.c_uint32)))
+    return re, lv
+
+
+def pava(g: Graph, k: int, level: np.ndarray) -> np.ndarray:
+    level = np.ascontiguousarray(level, dtype=np.uint32)
+    tent = np.empty(g.n, dtype=np.uint64)
+    _check(_lib.kclpp_pava(g.ctx.handle, g._h, k, _ptr(level, C.c_uint32), _ptr(tent, C.c_uint64)))
+    return tent
+
+
+def extract_densest_seq(g: Graph, k: int, T: int, r: np.ndarray) -> tuple[DensestInfo, np.ndarray]:
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    info = DensestInfo()
+    re = np.empty(g.n, dtype=np.uint32)
+    _check(_lib.kclpp_extract_densest_seq(g.ctx.handle, g._h, k, T, _ptr(r, C.c_uint64), C.byref(info),
+                                          _ptr(re, C.c_uint32)))
+    return info, re
+
+
+def extract_densest_sim(g: Graph, k: int, rho: np.ndarray) -> tuple[DensestInfo, np.ndarray]:
+    rho = np.ascontiguousarray(rho, dtype=np.float64)
+    info = DensestInfo()
+    re = np.empty(g.n, dtype=np.uint32)
+    _check(_lib.kclpp_extract_densest_sim(g.ctx.handle, g._h, k, _ptr(rho, C.c_double), C.byref(info),
+                                          _ptr(re, C.c_uint32)))
+    return info, re
+
+
+def _n_infos(num_iter: int) -> int:
+    c, T = 0, 1
+    while T <= num_iter:
+        c += 1
+        T <<= 1
+    return c
+
+
+def seq_main(g: Graph, k: int, num_iter: int, det_mode: int = SEQ_EDGE_STREAMS):
+    cap = max(1, _n_infos(num_iter))
+    infos = (DensestInfo * cap)()
+    r = np.zeros(g.n, dtype=np.uint64)
+    made = C.c_int()
+    _check(_lib.kclpp_seq_main(g.ctx.handle, g._h, k, num_iter, det_mode, _ptr(r, C.c_uint64), infos, cap,
+                               C.byref(made)))
+    return [infos[i] for i in range(made.value)], r
+
+
+def sim_main(g: Graph, k: int, num_iter: int):
+    cap = max(1, _n_infos(num_iter))
+    infos = (DensestInfo * cap)()
+    rho = np.zeros(g.n, dtype=np.float64)
+    made = C.c_int()
+    _check(_lib.kclpp_sim_main(g.ctx.handle, g._h, k, num_iter, _ptr(rho, C.c_double), infos, cap,
+                               C.byref(made)))
+    return [infos[i] for i in range(made.value)], rho
+
+
+@dataclass
+class TrimResult:
+    info: TrimInfo
+    map: np.ndarray        # new label -> original id
+    nck: np.ndarray        # k-clique degree per new label
+    order: np.ndarray      # peel order (new labels)
+    core_num: np.ndarray   # core number along the peel order
+    edges: EdgeList        # trimmed graph, original ids, input order
+
+
+def trim(ctx: Context, el: EdgeList, k: int, mode: int = TRIM_EXACT) -> TrimResult:
+    h = _P()
+    _check(_lib.kclpp_trim(ctx.handle, el._h, k, mode, C.byref(h)))
+    try:
+        info = TrimInfo()
+        _check(_lib.kclpp_trim_info_get(h, C.byref(info)))
+        n2 = info.n2
+        mp = np.empty(n2, dtype=np.uint32)
+        nck = np.empty(n2, dtype=np.uint64)
+        order = np.empty(n2, dtype=np.uint32)
+        core = np.empty(n2, dtype=np.uint64)
+        _check(_lib.kclpp_trim_copy(h, _ptr(mp, C.c_uint32), _ptr(nck, C.c_uint64), _ptr(order, C.c_uint32),
+                                    _ptr(core, C.c_uint64)))
+        eh = _P()
+        _check(_lib.kclpp_trim_edges(h, C.byref(eh)))
+        return TrimResult(info, mp, nck, order, core, EdgeList(eh))
+    finally:
+        _lib.kclpp_trim_free(h)

@@ -1,0 +1,816 @@
+// kclpp_api.cu -- the C ABI: contexts, device graphs, passes, extraction, trim.
+//
+// Data layout in HBM, per graph: the DAG out-CSR (offsets u64[n+1], cols
+// u32[m], ascending rows, cols < row), the source of every edge (u32[m], for
+// the edge-parallel CountEdges), and the root schedule: every vertex with an
+// out-edge, split into tiers by out-degree and sorted by descending estimated
+// work inside each tier.  Per-pass vectors (r, counts, level) live in a
+// workspace owned by the graph and reused across calls.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <numeric>
+
+#include "kclpp_dev.cuh"
+#include "kclpp_internal.h"
+
+namespace kclpp {
+const char *last_error_cstr();
+}
+using namespace kclpp;
+
+#define KCL_CUDA(call)                                                                        \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      return set_error(e_ == cudaErrorMemoryAllocation ? KCLPP_ERR_NOMEM : KCLPP_ERR_CUDA,    \
+                       "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);  \
+  } while (0)
+
+#define KCL_TRY(call)                      \
+  do {                                     \
+    kclpp_status s_ = (call);              \
+    if (s_ != KCLPP_OK) return s_;         \
+  } while (0)
+
+struct kclpp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 1;
+  uint32_t *d_err = nullptr;
+  uint64_t launches = 0;
+};
+
+struct TierInfo {
+  int tier;
+  uint32_t offset, count, dmax;
+};
+
+struct kclpp_graph {
+  int device = 0;
+  HostDag dag;
+  uint64_t *d_off = nullptr;
+  uint32_t *d_cols = nullptr;
+  uint32_t *d_src = nullptr;
+  uint32_t *d_roots = nullptr;
+  std::vector<TierInfo> tiers;
+  uint32_t maxdeg = 0;
+  // workspace
+  unsigned long long *d_a = nullptr, *d_b = nullptr;
+  double *d_rho = nullptr;
+  uint32_t *d_level = nullptr;
+  uint32_t *d_work = nullptr;
+  unsigned long long *d_scalar = nullptr;
+  uint32_t *d_slab = nullptr;
+  uint64_t slab_words = 0;
+  int slab_ctas = 0;
+};
+
+// ---------------------------------------------------------------------------
+// small device helpers
+namespace {
+
+__global__ void k_sim_update(double *rho, const unsigned long long *cnt, uint32_t n, uint32_t t) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // rho = (t * rho + 2.0 * rho_add) / (t + 2.0), each operation rounded
+  // separately (kCDensestCmpSync.c:403); rho_add is an exact integer.
+  const double td = __uint2double_rn(t);
+  const double add = __ull2double_rn(cnt[i]);
+  rho[i] = __ddiv_rn(__dadd_rn(__dmul_rn(td, rho[i]), __dmul_rn(2.0, add)), __dadd_rn(td, 2.0));
+}
+
+__global__ void k_scatter_level(unsigned long long *tent, const unsigned long long *cnt, const uint32_t *level,
+                                uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) tent[level[i]] = cnt[i];
+}
+
+__global__ void k_count_edges(const uint32_t *src, const uint32_t *cols, uint64_t m, const uint32_t *level,
+                              uint32_t nstar, unsigned long long *out) {
+  unsigned long long c = 0;
+  for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x)
+    c += (level[src[e]] < nstar && level[cols[e]] < nstar);
+  c = dev::warp_sum(c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+inline int blocks_for(uint64_t n, int t = 256) { return (int)std::max<uint64_t>(1, (n + t - 1) / t); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+static kclpp_status check_err(kclpp_ctx *c) {
+  uint32_t e = 0;
+  KCL_CUDA(cudaMemcpyAsync(&e, c->d_err, sizeof e, cudaMemcpyDeviceToHost, c->stream));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  if (e) {
+    KCL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+    if (e & dev::ERR_OVERFLOW) return set_error(KCLPP_ERR_OVERFLOW, "a per-stream 32-bit counter would have wrapped");
+    if (e & dev::ERR_DEGREE) return set_error(KCLPP_ERR_UNSUPPORTED, "a root's out-degree exceeds its tier");
+    return set_error(KCLPP_ERR_CUDA, "device status word 0x%x", e);
+  }
+  return KCLPP_OK;
+}
+
+static kclpp_status set_device(kclpp_ctx *c) {
+  KCL_CUDA(cudaSetDevice(c->device));
+  return KCLPP_OK;
+}
+
+template <typename T>
+static kclpp_status dalloc(T **p, size_t count) {
+  if (*p) return KCLPP_OK;
+  KCL_CUDA(cudaMalloc((void **)p, std::max<size_t>(count, 1) * sizeof(T)));
+  return KCLPP_OK;
+}
+
+// Root schedule: tiers by out-degree, descending work (out-degree squared,
+// then id) inside each tier.
+static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
+  const HostDag &D = g->dag;
+  std::vector<uint32_t> tS, tM1, tM2, tM3, tL;
+  uint32_t mx = 0;
+  for (uint32_t s = 0; s < D.n; ++s) {
+    const uint32_t d = (uint32_t)(D.off[s + 1] - D.off[s]);
+    if (d == 0) continue;
+    mx = std::max(mx, d);
+    if (d <= kTierSMax) tS.push_back(s);
+    else if (d <= 256) tM1.push_back(s);
+    else if (d <= 512) tM2.push_back(s);
+    else if (d <= kTierMMax) tM3.push_back(s);
+    else tL.push_back(s);
+  }
+  g->maxdeg = mx;
+  auto deg = [&](uint32_t s) { return (uint32_t)(D.off[s + 1] - D.off[s]); };
+  auto by_work = [&](uint32_t a, uint32_t b) {
+    const uint32_t da = deg(a), db = deg(b);
+    return da != db ? da > db : a < b;
+  };
+  std::vector<uint32_t> all;
+  g->tiers.clear();
+  auto add = [&](std::vector<uint32_t> &v, int tier) {
+    if (v.empty()) return;
+    std::sort(v.begin(), v.end(), by_work);
+    TierInfo t;
+    t.tier = tier;
+    t.offset = (uint32_t)all.size();
+    t.count = (uint32_t)v.size();
+    t.dmax = deg(v.front());
+    all.insert(all.end(), v.begin(), v.end());
+    g->tiers.push_back(t);
+  };
+  // Largest roots first so that their long CTAs start early.
+  add(tL, 2);
+  add(tM3, 1);
+  add(tM2, 1);
+  add(tM1, 1);
+  add(tS, 0);
+  KCL_TRY(dalloc(&g->d_roots, all.size()));
+  if (!all.empty())
+    KCL_CUDA(cudaMemcpyAsync(g->d_roots, all.data(), all.size() * 4, cudaMemcpyHostToDevice, c->stream));
+  KCL_TRY(dalloc(&g->d_work, 16));
+  if (!tL.empty()) {
+    g->slab_ctas = c->num_sms;
+    const uint64_t W = (kTierLMax + 31) / 32;
+    g->slab_words = (uint64_t)kTierLMax * W;
+    KCL_TRY(dalloc(&g->d_slab, g->slab_words * g->slab_ctas));
+  }
+  return KCLPP_OK;
+}
+
+static kclpp_status upload_graph(kclpp_ctx *c, kclpp_graph *g) {
+  const HostDag &D = g->dag;
+  if (D.core > kTierLMax)
+    return set_error(KCLPP_ERR_UNSUPPORTED, "max out-degree %u exceeds the supported %u", D.core, kTierLMax);
+  KCL_TRY(dalloc(&g->d_off, (size_t)D.n + 1));
+  KCL_TRY(dalloc(&g->d_cols, D.m()));
+  KCL_TRY(dalloc(&g->d_src, D.m()));
+  KCL_CUDA(cudaMemcpyAsync(g->d_off, D.off.data(), ((size_t)D.n + 1) * 8, cudaMemcpyHostToDevice, c->stream));
+  if (D.m()) {
+    KCL_CUDA(cudaMemcpyAsync(g->d_cols, D.cols.data(), D.m() * 4, cudaMemcpyHostToDevice, c->stream));
+    std::vector<uint32_t> src(D.m());
+    for (uint32_t s = 0; s < D.n; ++s)
+      for (uint64_t e = D.off[s]; e < D.off[s + 1]; ++e) src[e] = s;
+    KCL_CUDA(cudaMemcpyAsync(g->d_src, src.data(), D.m() * 4, cudaMemcpyHostToDevice, c->stream));
+    KCL_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  KCL_TRY(build_schedule(c, g));
+  const size_t n1 = (size_t)D.n + 1;
+  KCL_TRY(dalloc(&g->d_a, n1));
+  KCL_TRY(dalloc(&g->d_b, n1));
+  KCL_TRY(dalloc(&g->d_rho, n1));
+  KCL_TRY(dalloc(&g->d_level, n1));
+  KCL_TRY(dalloc(&g->d_scalar, 4));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  return KCLPP_OK;
+}
+
+static void free_graph_dev(kclpp_graph *g) {
+  cudaFree(g->d_off); cudaFree(g->d_cols); cudaFree(g->d_src); cudaFree(g->d_roots);
+  cudaFree(g->d_a); cudaFree(g->d_b); cudaFree(g->d_rho); cudaFree(g->d_level);
+  cudaFree(g->d_work); cudaFree(g->d_scalar); cudaFree(g->d_slab);
+}
+
+// Launch every tier of one mode.
+static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev::PassArgs a) {
+  if (g->tiers.empty()) return KCLPP_OK;
+  KCL_CUDA(cudaMemsetAsync(g->d_work, 0, 16 * sizeof(uint32_t), c->stream));
+  a.off = g->d_off;
+  a.cols = g->d_cols;
+  a.err = c->d_err;
+  a.slab = g->d_slab;
+  a.slab_words = g->slab_words;
+  for (size_t i = 0; i < g->tiers.size(); ++i) {
+    const TierInfo &t = g->tiers[i];
+    TierLaunch tl;
+    tl.tier = t.tier;
+    tl.roots = g->d_roots + t.offset;
+    tl.num_roots = t.count;
+    tl.dmax = t.dmax;
+    tl.work = g->d_work + i;
+    tl.num_sms = c->num_sms;
+    tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
+    cudaError_t e = cudaSuccess;
+    if (mode == dev::MODE_COUNT) e = launch_count(k, tl, a, c->stream);
+    else if (mode == dev::MODE_ORDER) e = launch_order(k, tl, a, c->stream);
+    else e = launch_seq(k, tl, a, c->stream);
+    if (e != cudaSuccess)
+      return set_error(KCLPP_ERR_CUDA, "kernel launch (mode %d, tier %d, k %d): %s", mode, t.tier, k,
+                       cudaGetErrorString(e));
+    c->launches++;
+  }
+  return KCLPP_OK;
+}
+
+// ---- device-resident passes (enqueue only) ---------------------------------
+static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsigned long long *in,
+                                 unsigned long long *out, unsigned long long *cliques) {
+  const uint32_t n = g->dag.n;
+  if (in != out) KCL_CUDA(cudaMemcpyAsync(out, in, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->stream));
+  dev::PassArgs a{};
+  a.r_in = in;
+  a.out = out;
+  a.cliques = cliques;
+  return run_tiers(c, g, dev::MODE_SEQ, k, a);
+}
+
+static kclpp_status sim_counts_dev(kclpp_ctx *c, kclpp_graph *g, int k, const double *rho, unsigned long long *cnt) {
+  KCL_CUDA(cudaMemsetAsync(cnt, 0, (size_t)g->dag.n * 8, c->stream));
+  dev::PassArgs a{};
+  a.key_kind = dev::KEY_SIM;
+  a.rho = rho;
+  a.out = cnt;
+  return run_tiers(c, g, dev::MODE_ORDER, k, a);
+}
+
+static kclpp_status sim_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t t, double *rho) {
+  KCL_TRY(sim_counts_dev(c, g, k, rho, g->d_a));
+  const uint32_t n = g->dag.n;
+  if (n) {
+    k_sim_update<<<blocks_for(n), 256, 0, c->stream>>>(rho, g->d_a, n, t);
+    KCL_CUDA(cudaGetLastError());
+    c->launches++;
+  }
+  return KCLPP_OK;
+}
+
+static kclpp_status pava_dev(kclpp_ctx *c, kclpp_graph *g, int k, const uint32_t *level_dev,
+                             unsigned long long *tent_dev) {
+  const uint32_t n = g->dag.n;
+  KCL_CUDA(cudaMemsetAsync(g->d_a, 0, (size_t)n * 8, c->stream));
+  dev::PassArgs a{};
+  a.key_kind = dev::KEY_LEVEL;
+  a.level = level_dev;
+  a.out = g->d_a;
+  KCL_TRY(run_tiers(c, g, dev::MODE_ORDER, k, a));
+  if (n) {
+    k_scatter_level<<<blocks_for(n), 256, 0, c->stream>>>(tent_dev, g->d_a, level_dev, n);
+    KCL_CUDA(cudaGetLastError());
+    c->launches++;
+  }
+  return KCLPP_OK;
+}
+
+static kclpp_status check_k(int k, int lo) {
+  if (k < lo || k > KCLPP_MAX_K)
+    return set_error(KCLPP_ERR_UNSUPPORTED, "k = %d outside the supported range [%d, %d]", k, lo, KCLPP_MAX_K);
+  return KCLPP_OK;
+}
+
+// ---- host-side pieces of the extraction (A10, A12, A13) --------------------
+struct KeyId {
+  uint64_t key;
+  uint32_t id;
+};
+static void sort_desc(uint32_t n, std::vector<KeyId> &v, uint32_t *reordered, uint32_t *level) {
+  std::sort(v.begin(), v.end(), [](const KeyId &a, const KeyId &b) {
+    return a.key != b.key ? a.key > b.key : a.id < b.id;
+  });
+  for (uint32_t i = 0; i < n; ++i) {
+    if (reordered) reordered[i] = v[i].id;
+    if (level) level[v[i].id] = i;
+  }
+}
+
+extern "C" {
+
+const char *kclpp_status_string(kclpp_status s) {
+  switch (s) {
+    case KCLPP_OK: return "ok";
+    case KCLPP_ERR_INVALID: return "invalid argument";
+    case KCLPP_ERR_IO: return "i/o error";
+    case KCLPP_ERR_NOMEM: return "out of memory";
+    case KCLPP_ERR_CUDA: return "cuda error";
+    case KCLPP_ERR_UNSUPPORTED: return "unsupported";
+    case KCLPP_ERR_OVERFLOW: return "counter overflow";
+    case KCLPP_ERR_NODEVICE: return "no cuda device";
+    default: return "unknown status";
+  }
+}
+const char *kclpp_last_error(void) { return last_error_cstr(); }
+const char *kclpp_version(void) { return "kclpp-gb300 0.1 (sm_103a)"; }
+
+kclpp_status kclpp_create(int device, void *stream, kclpp_ctx **out) {
+  if (!out) return set_error(KCLPP_ERR_INVALID, "kclpp_create: null out");
+  *out = nullptr;
+  int nd = 0;
+  cudaError_t e = cudaGetDeviceCount(&nd);
+  if (e != cudaSuccess || nd == 0) return set_error(KCLPP_ERR_NODEVICE, "no CUDA device (%s)", cudaGetErrorString(e));
+  if (device < 0 || device >= nd) return set_error(KCLPP_ERR_INVALID, "device %d out of range", device);
+  std::unique_ptr<kclpp_ctx> c(new kclpp_ctx());
+  c->device = device;
+  KCL_CUDA(cudaSetDevice(device));
+  KCL_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    KCL_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    c->own_stream = true;
+  }
+  KCL_CUDA(cudaMalloc((void **)&c->d_err, sizeof(uint32_t)));
+  KCL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  *out = c.release();
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_destroy(kclpp_ctx *c) {
+  if (!c) return KCLPP_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_err);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_synchronize(kclpp_ctx *c) {
+  if (!c) return set_error(KCLPP_ERR_INVALID, "null context");
+  KCL_TRY(set_device(c));
+  return check_err(c);
+}
+
+uint64_t kclpp_launch_count(const kclpp_ctx *c) { return c ? c->launches : 0; }
+
+// ---- graphs -------------------------------------------------------------------
+kclpp_status kclpp_core_order(const kclpp_edge_list *el, uint32_t *rank_out) {
+  if (!el || !rank_out) return set_error(KCLPP_ERR_INVALID, "kclpp_core_order: null argument");
+  core_order_host(el->n, el->pairs, rank_out);
+  return KCLPP_OK;
+}
+
+static kclpp_status finish_graph(kclpp_ctx *c, kclpp_graph *gp, kclpp_graph **out) {
+  std::unique_ptr<kclpp_graph> g(gp);
+  g->device = c->device;
+  kclpp_status s = upload_graph(c, g.get());
+  if (s != KCLPP_OK) {
+    free_graph_dev(g.get());
+    return s;
+  }
+  *out = g.release();
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_make_graph(kclpp_ctx *c, const kclpp_edge_list *el, const uint32_t *rank, kclpp_graph **out) {
+  if (!c || !el || !rank || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_make_graph: null argument");
+  *out = nullptr;
+  KCL_TRY(set_device(c));
+  auto *g = new kclpp_graph();
+  kclpp_status s = make_dag_host(el->pairs, rank, g->dag);
+  if (s != KCLPP_OK) { delete g; return s; }
+  return finish_graph(c, g, out);
+}
+
+kclpp_status kclpp_build_graph(kclpp_ctx *c, const kclpp_edge_list *el, kclpp_graph **out) {
+  if (!c || !el || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_build_graph: null argument");
+  std::vector<uint32_t> rank(el->n);
+  KCL_TRY(kclpp_core_order(el, rank.data()));
+  return kclpp_make_graph(c, el, rank.data(), out);
+}
+
+kclpp_status kclpp_graph_from_csr(kclpp_ctx *c, uint32_t n, uint64_t m, const uint64_t *offsets,
+                                  const uint32_t *cols, kclpp_graph **out) {
+  if (!c || !offsets || (!cols && m) || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_graph_from_csr: null argument");
+  *out = nullptr;
+  if (offsets[0] != 0 || offsets[n] != m) return set_error(KCLPP_ERR_INVALID, "offsets[0] must be 0 and offsets[n] = m");
+  KCL_TRY(set_device(c));
+  auto *g = new kclpp_graph();
+  g->dag.n = n;
+  g->dag.off.assign(offsets, offsets + n + 1);
+  g->dag.cols.assign(cols, cols + m);
+  uint32_t mx = 0;
+  for (uint32_t s = 0; s < n; ++s) {
+    if (offsets[s + 1] < offsets[s]) { delete g; return set_error(KCLPP_ERR_INVALID, "offsets not monotone at %u", s); }
+    mx = std::max<uint32_t>(mx, (uint32_t)(offsets[s + 1] - offsets[s]));
+    for (uint64_t e = offsets[s]; e < offsets[s + 1]; ++e) {
+      if (cols[e] >= s || (e > offsets[s] && cols[e] <= cols[e - 1])) {
+        delete g;
+        return set_error(KCLPP_ERR_INVALID, "row %u is not strictly ascending below the source", s);
+      }
+    }
+  }
+  g->dag.core = mx;
+  return finish_graph(c, g, out);
+}
+
+kclpp_status kclpp_graph_info(const kclpp_graph *g, uint32_t *n, uint64_t *m, uint32_t *core) {
+  if (!g) return set_error(KCLPP_ERR_INVALID, "null graph");
+  if (n) *n = g->dag.n;
+  if (m) *m = g->dag.m();
+  if (core) *core = g->dag.core;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_graph_copy_csr(const kclpp_graph *g, uint64_t *offsets, uint32_t *cols) {
+  if (!g) return set_error(KCLPP_ERR_INVALID, "null graph");
+  if (offsets) memcpy(offsets, g->dag.off.data(), g->dag.off.size() * 8);
+  if (cols && g->dag.m()) memcpy(cols, g->dag.cols.data(), g->dag.m() * 4);
+  return KCLPP_OK;
+}
+
+void kclpp_graph_free(kclpp_graph *g) {
+  if (!g) return;
+  cudaSetDevice(g->device);
+  free_graph_dev(g);
+  delete g;
+}
+
+// ---- counts ---------------------------------------------------------------------
+kclpp_status kclpp_count_cliques(kclpp_ctx *c, const kclpp_graph *gc, int k, uint64_t *per_vertex, uint64_t *total) {
+  if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const uint32_t n = g->dag.n;
+  KCL_CUDA(cudaMemsetAsync(g->d_a, 0, (size_t)n * 8 + 8, c->stream));
+  dev::PassArgs a{};
+  a.out = g->d_a;
+  KCL_TRY(run_tiers(c, g, dev::MODE_COUNT, k, a));
+  KCL_TRY(check_err(c));
+  std::vector<uint64_t> h(n);
+  if (n) KCL_CUDA(cudaMemcpyAsync(h.data(), g->d_a, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  unsigned __int128 sum = 0;
+  for (uint64_t v : h) sum += v;
+  if (per_vertex && n) memcpy(per_vertex, h.data(), (size_t)n * 8);
+  if (total) *total = (uint64_t)(sum / (unsigned)k);
+  return KCLPP_OK;
+}
+
+// ---- Seq --------------------------------------------------------------------------
+static kclpp_status seq_passes_on(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t passes, unsigned long long *r) {
+  // Ping-pong between r and the workspace; end with the result in r.
+  unsigned long long *in = r, *out = g->d_b;
+  for (uint32_t p = 0; p < passes; ++p) {
+    KCL_TRY(seq_pass_dev(c, g, k, in, out, nullptr));
+    std::swap(in, out);
+  }
+  if (in != r) KCL_CUDA(cudaMemcpyAsync(r, in, (size_t)g->dag.n * 8, cudaMemcpyDeviceToDevice, c->stream));
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_seq_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t passes, int det_mode,
+                                  uint64_t *r_dev) {
+  if (!c || !gc || (!r_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  if (det_mode != KCLPP_SEQ_EDGE_STREAMS) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  KCL_TRY(set_device(c));
+  return seq_passes_on(c, const_cast<kclpp_graph *>(gc), k, passes, (unsigned long long *)r_dev);
+}
+
+kclpp_status kclpp_seq_passes(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t passes, int det_mode,
+                              uint64_t *r) {
+  if (!c || !gc || (!r && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  if (det_mode != KCLPP_SEQ_EDGE_STREAMS) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const size_t bytes = (size_t)g->dag.n * 8;
+  if (!bytes) return KCLPP_OK;
+  KCL_CUDA(cudaMemcpyAsync(g->d_a, r, bytes, cudaMemcpyHostToDevice, c->stream));
+  KCL_TRY(seq_passes_on(c, g, k, passes, g->d_a));
+  KCL_CUDA(cudaMemcpyAsync(r, g->d_a, bytes, cudaMemcpyDeviceToHost, c->stream));
+  return check_err(c);
+}
+
+kclpp_status kclpp_seq_passes_csr(kclpp_ctx *c, uint32_t n, uint64_t m, const uint64_t *offsets, const uint32_t *cols,
+                                  int k, uint32_t passes, int det_mode, uint64_t *r) {
+  kclpp_graph *g = nullptr;
+  KCL_TRY(kclpp_graph_from_csr(c, n, m, offsets, cols, &g));
+  kclpp_status s = kclpp_seq_passes(c, g, k, passes, det_mode, r);
+  kclpp_graph_free(g);
+  return s;
+}
+
+// ---- Sim --------------------------------------------------------------------------
+kclpp_status kclpp_sim_counts(kclpp_ctx *c, const kclpp_graph *gc, int k, const double *rho, uint64_t *cnt) {
+  if (!c || !gc || ((!rho || !cnt) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const size_t bytes = (size_t)g->dag.n * 8;
+  if (!bytes) return KCLPP_OK;
+  KCL_CUDA(cudaMemcpyAsync(g->d_rho, rho, bytes, cudaMemcpyHostToDevice, c->stream));
+  KCL_TRY(sim_counts_dev(c, g, k, g->d_rho, g->d_a));
+  KCL_CUDA(cudaMemcpyAsync(cnt, g->d_a, bytes, cudaMemcpyDeviceToHost, c->stream));
+  return check_err(c);
+}
+
+kclpp_status kclpp_sim_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t t_first, uint32_t passes,
+                                  double *rho_dev) {
+  if (!c || !gc || (!rho_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  if (t_first < 1) return set_error(KCLPP_ERR_INVALID, "t_first must be >= 1");
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  for (uint32_t p = 0; p < passes; ++p) KCL_TRY(sim_pass_dev(c, g, k, t_first + p, rho_dev));
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_sim_passes(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t t_first, uint32_t passes,
+                              double *rho) {
+  if (!c || !gc || (!rho && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  if (t_first < 1) return set_error(KCLPP_ERR_INVALID, "t_first must be >= 1");
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const size_t bytes = (size_t)g->dag.n * 8;
+  if (!bytes) return KCLPP_OK;
+  KCL_CUDA(cudaMemcpyAsync(g->d_rho, rho, bytes, cudaMemcpyHostToDevice, c->stream));
+  for (uint32_t p = 0; p < passes; ++p) KCL_TRY(sim_pass_dev(c, g, k, t_first + p, g->d_rho));
+  KCL_CUDA(cudaMemcpyAsync(rho, g->d_rho, bytes, cudaMemcpyDeviceToHost, c->stream));
+  return check_err(c);
+}
+
+kclpp_status kclpp_sim_passes_csr(kclpp_ctx *c, uint32_t n, uint64_t m, const uint64_t *offsets, const uint32_t *cols,
+                                  int k, uint32_t t_first, uint32_t passes, double *rho) {
+  kclpp_graph *g = nullptr;
+  KCL_TRY(kclpp_graph_from_csr(c, n, m, offsets, cols, &g));
+  kclpp_status s = kclpp_sim_passes(c, g, k, t_first, passes, rho);
+  kclpp_graph_free(g);
+  return s;
+}
+
+// ---- sort, PAVA, densest prefix ------------------------------------------------------
+kclpp_status kclpp_sort_by_r_u64(kclpp_ctx *c, uint32_t n, const uint64_t *r, uint32_t *reordered, uint32_t *level) {
+  (void)c;
+  if (!r && n) return set_error(KCLPP_ERR_INVALID, "null r");
+  std::vector<KeyId> v(n);
+  for (uint32_t i = 0; i < n; ++i) v[i] = {r[i], i};
+  sort_desc(n, v, reordered, level);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_sort_by_r_f64(kclpp_ctx *c, uint32_t n, const double *r, uint32_t *reordered, uint32_t *level) {
+  (void)c;
+  if (!r && n) return set_error(KCLPP_ERR_INVALID, "null r");
+  std::vector<KeyId> v(n);
+  for (uint32_t i = 0; i < n; ++i) v[i] = {(uint64_t)(unsigned long long)r[i], i};  // (unsigned long long)rho
+  sort_desc(n, v, reordered, level);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_pava(kclpp_ctx *c, const kclpp_graph *gc, int k, const uint32_t *level, uint64_t *tentative) {
+  if (!c || !gc || ((!level || !tentative) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const uint32_t n = g->dag.n;
+  if (!n) return KCLPP_OK;
+  KCL_CUDA(cudaMemcpyAsync(g->d_level, level, (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  KCL_TRY(pava_dev(c, g, k, g->d_level, g->d_b));
+  KCL_CUDA(cudaMemcpyAsync(tentative, g->d_b, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+  return check_err(c);
+}
+
+kclpp_status kclpp_count_edges(kclpp_ctx *c, const kclpp_graph *gc, uint32_t num_nodes, const uint32_t *nodes,
+                               uint32_t *m_out) {
+  if (!c || !gc || !m_out || (!nodes && num_nodes)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const uint32_t n = g->dag.n;
+  // level[v] = position among nodes (n for vertices not listed); CountEdges
+  // then keeps the edges with both ends below num_nodes.
+  std::vector<uint32_t> lv(n, UINT32_MAX);
+  for (uint32_t i = 0; i < num_nodes; ++i) {
+    if (nodes[i] >= n) return set_error(KCLPP_ERR_INVALID, "node id %u out of range", nodes[i]);
+    lv[nodes[i]] = 0;
+  }
+  if (!n) { *m_out = 0; return KCLPP_OK; }
+  KCL_CUDA(cudaMemcpyAsync(g->d_level, lv.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  KCL_CUDA(cudaMemsetAsync(g->d_scalar, 0, 8, c->stream));
+  const uint64_t m = g->dag.m();
+  if (m) {
+    k_count_edges<<<std::min(blocks_for(m), c->num_sms * 8), 256, 0, c->stream>>>(g->d_src, g->d_cols, m,
+                                                                               g->d_level, 1u, g->d_scalar);
+    KCL_CUDA(cudaGetLastError());
+    c->launches++;
+  }
+  unsigned long long h = 0;
+  KCL_CUDA(cudaMemcpyAsync(&h, g->d_scalar, 8, cudaMemcpyDeviceToHost, c->stream));
+  KCL_TRY(check_err(c));
+  *m_out = (uint32_t)h;
+  return KCLPP_OK;
+}
+
+// Shared tail of both extractions: PAVA pass on the device, CountEdges.
+static kclpp_status pava_and_edges(kclpp_ctx *c, kclpp_graph *g, int k, const std::vector<uint32_t> &level,
+                                   std::vector<uint64_t> &tent) {
+  const uint32_t n = g->dag.n;
+  KCL_CUDA(cudaMemcpyAsync(g->d_level, level.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  KCL_TRY(pava_dev(c, g, k, g->d_level, g->d_b));
+  tent.resize(n);
+  KCL_CUDA(cudaMemcpyAsync(tent.data(), g->d_b, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+  return check_err(c);
+}
+
+static kclpp_status edges_in_prefix(kclpp_ctx *c, kclpp_graph *g, uint32_t nstar, uint32_t *m_out) {
+  KCL_CUDA(cudaMemsetAsync(g->d_scalar, 0, 8, c->stream));
+  const uint64_t m = g->dag.m();
+  if (m) {
+    k_count_edges<<<std::min(blocks_for(m), c->num_sms * 8), 256, 0, c->stream>>>(g->d_src, g->d_cols, m,
+                                                                               g->d_level, nstar, g->d_scalar);
+    KCL_CUDA(cudaGetLastError());
+    c->launches++;
+  }
+  unsigned long long h = 0;
+  KCL_CUDA(cudaMemcpyAsync(&h, g->d_scalar, 8, cudaMemcpyDeviceToHost, c->stream));
+  KCL_TRY(check_err(c));
+  *m_out = (uint32_t)h;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_extract_densest_seq(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t T, const uint64_t *r,
+                                       kclpp_densest_info *info, uint32_t *reordered_out) {
+  if (!c || !gc || !info || (!r && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  if (T < 1) return set_error(KCLPP_ERR_INVALID, "T must be >= 1");
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  memset(info, 0, sizeof *info);
+  const uint32_t n = g->dag.n;
+  if (!n) return KCLPP_OK;
+  std::vector<uint32_t> reordered(n), level(n);
+  KCL_TRY(kclpp_sort_by_r_u64(c, n, r, reordered.data(), level.data()));
+  std::vector<uint64_t> tent;
+  KCL_TRY(pava_and_edges(c, g, k, level, tent));
+  // kCDensestNoAtom.c:342-349: first strictly largest prefix density.
+  double density = -1;
+  unsigned long long sum = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += tent[i];
+    if ((double)sum / (i + 1) > density) {
+      density = (double)sum / (i + 1);
+      info->n = i + 1;
+      info->cliques = sum;
+    }
+  }
+  info->density = density;
+  KCL_TRY(edges_in_prefix(c, g, info->n, &info->m));
+  // kCDensestNoAtom.c:352-369
+  sum = 0;
+  double ub = 0, ip1ck = 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += r[reordered[i]];
+    if (i + 1 == (uint32_t)k) ip1ck = 1;
+    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
+    if (ip1ck < (double)sum / T) ub = ip1ck / (i + 1);
+    else {
+      if (ub < (double)sum / T / (i + 1)) ub = (double)sum / T / (i + 1);
+      break;
+    }
+  }
+  info->ub = ub;
+  if (reordered_out) memcpy(reordered_out, reordered.data(), (size_t)n * 4);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_extract_densest_sim(kclpp_ctx *c, const kclpp_graph *gc, int k, const double *rho,
+                                       kclpp_densest_info *info, uint32_t *reordered_out) {
+  if (!c || !gc || !info || (!rho && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  memset(info, 0, sizeof *info);
+  const uint32_t n = g->dag.n;
+  if (!n) return KCLPP_OK;
+  std::vector<uint32_t> reordered(n), level(n);
+  KCL_TRY(kclpp_sort_by_r_f64(c, n, rho, reordered.data(), level.data()));
+  std::vector<uint64_t> tent;
+  KCL_TRY(pava_and_edges(c, g, k, level, tent));
+  // kCDensestCmpSync.c:354-361 (double accumulator)
+  double density = -1, sum = 0;
+  uint64_t isum = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += (double)tent[i];
+    isum += tent[i];
+    if (sum / (i + 1) > density) {
+      density = sum / (i + 1);
+      info->n = i + 1;
+      info->cliques = isum;
+    }
+  }
+  info->density = density;
+  KCL_TRY(edges_in_prefix(c, g, info->n, &info->m));
+  // kCDensestCmpSync.c:365-381
+  sum = 0;
+  double ub = 0, ip1ck = 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += rho[reordered[i]];
+    if (i + 1 == (uint32_t)k) ip1ck = 1;
+    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
+    if (ip1ck < sum) ub = ip1ck / (i + 1);
+    else {
+      if (ub < sum / (i + 1)) ub = sum / (i + 1);
+      break;
+    }
+  }
+  info->ub = ub;
+  if (reordered_out) memcpy(reordered_out, reordered.data(), (size_t)n * 4);
+  return KCLPP_OK;
+}
+
+// ---- whole runs ------------------------------------------------------------------------
+kclpp_status kclpp_seq_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t num_iter, int det_mode,
+                            uint64_t *r_out, kclpp_densest_info *infos, int max_infos, int *n_infos) {
+  if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  if (det_mode != KCLPP_SEQ_EDGE_STREAMS) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const uint32_t n = g->dag.n;
+  std::vector<uint64_t> r(n, 0);
+  int made = 0;
+  unsigned long long *dr = nullptr;
+  KCL_CUDA(cudaMalloc((void **)&dr, std::max<size_t>((size_t)n * 8, 8)));
+  std::unique_ptr<unsigned long long, decltype(&cudaFree)> guard(dr, &cudaFree);
+  if (n) KCL_CUDA(cudaMemsetAsync(dr, 0, (size_t)n * 8, c->stream));
+  for (uint32_t T = 1, t = 1; T <= num_iter; T <<= 1) {
+    if (T > t - 1) {
+      KCL_TRY(seq_passes_on(c, g, k, T - (t - 1), dr));
+      t = T + 1;
+    }
+    if (n) KCL_CUDA(cudaMemcpyAsync(r.data(), dr, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+    KCL_TRY(check_err(c));
+    kclpp_densest_info info;
+    KCL_TRY(kclpp_extract_densest_seq(c, g, k, T, r.data(), &info, nullptr));
+    if (infos && made < max_infos) infos[made] = info;
+    ++made;
+    if (T > (UINT32_MAX >> 1)) break;
+  }
+  if (r_out && n) memcpy(r_out, r.data(), (size_t)n * 8);
+  if (n_infos) *n_infos = made;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_sim_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t num_iter, double *rho_out,
+                            kclpp_densest_info *infos, int max_infos, int *n_infos) {
+  if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const uint32_t n = g->dag.n;
+  std::vector<double> rho(n, 0.0);
+  int made = 0;
+  if (n) KCL_CUDA(cudaMemsetAsync(g->d_rho, 0, (size_t)n * 8, c->stream));
+  for (uint32_t T = 1, t = 1; T <= num_iter; T <<= 1) {
+    for (; t <= T; ++t) KCL_TRY(sim_pass_dev(c, g, k, t, g->d_rho));
+    if (n) KCL_CUDA(cudaMemcpyAsync(rho.data(), g->d_rho, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));
+    KCL_TRY(check_err(c));
+    kclpp_densest_info info;
+    KCL_TRY(kclpp_extract_densest_sim(c, g, k, rho.data(), &info, nullptr));
+    if (infos && made < max_infos) infos[made] = info;
+    ++made;
+    if (T > (UINT32_MAX >> 1)) break;
+  }
+  if (rho_out && n) memcpy(rho_out, rho.data(), (size_t)n * 8);
+  if (n_infos) *n_infos = made;
+  return KCLPP_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,315 @@
+// kclpp_gen.cpp -- edge-list I/O and seeded synthetic graph generators.
+//
+// Input side of the path: ReadEdgeList (Graph.c:34-53) and the seeded graphs
+// that stand in for the paper's datasets (Chung-Lu, RMAT, Erdos-Renyi, planted
+// dense communities).  All arithmetic is plain IEEE double with no fused
+// multiply-add (the library is built with -ffp-contract=off), so a seed gives
+// the same graph on x86 and Arm hosts.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+
+#include "kclpp_internal.h"
+
+namespace kclpp {
+
+static thread_local std::string g_last_error;
+
+kclpp_status set_error(kclpp_status s, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return s;
+}
+void clear_error() { g_last_error.clear(); }
+const char *last_error_cstr() { return g_last_error.c_str(); }
+
+void radix_sort_u64(std::vector<uint64_t> &keys) {
+  const size_t n = keys.size();
+  if (n < 2) return;
+  uint64_t orv = 0, andv = ~0ull;
+  for (uint64_t k : keys) { orv |= k; andv &= k; }
+  const uint64_t vary = orv ^ andv;
+  std::vector<uint64_t> tmp(n);
+  std::vector<size_t> cnt(1 << 16);
+  for (int shift = 0; shift < 64; shift += 16) {
+    if (((vary >> shift) & 0xFFFFull) == 0) continue;
+    std::fill(cnt.begin(), cnt.end(), 0);
+    for (uint64_t k : keys) cnt[(k >> shift) & 0xFFFF]++;
+    size_t sum = 0;
+    for (auto &c : cnt) { size_t t = c; c = sum; sum += t; }
+    for (uint64_t k : keys) tmp[cnt[(k >> shift) & 0xFFFF]++] = k;
+    keys.swap(tmp);
+  }
+}
+
+// Vose alias table for O(1) weighted sampling.
+struct Alias {
+  std::vector<double> prob;
+  std::vector<uint32_t> alias;
+  explicit Alias(const std::vector<double> &w) {
+    const size_t n = w.size();
+    prob.assign(n, 0.0);
+    alias.assign(n, 0);
+    double total = 0;
+    for (double x : w) total += x;
+    std::vector<double> p(n);
+    std::vector<uint32_t> small, large;
+    for (size_t i = 0; i < n; ++i) {
+      p[i] = w[i] * (double)n / total;
+      (p[i] < 1.0 ? small : large).push_back((uint32_t)i);
+    }
+    while (!small.empty() && !large.empty()) {
+      uint32_t s = small.back(); small.pop_back();
+      uint32_t l = large.back(); large.pop_back();
+      prob[s] = p[s];
+      alias[s] = l;
+      p[l] = (p[l] + p[s]) - 1.0;
+      (p[l] < 1.0 ? small : large).push_back(l);
+    }
+    for (uint32_t l : large) prob[l] = 1.0;
+    for (uint32_t s : small) prob[s] = 1.0;
+  }
+  inline uint32_t draw(SplitMix &r) const {
+    uint32_t i = (uint32_t)r.below(prob.size());
+    return r.uniform() < prob[i] ? i : alias[i];
+  }
+};
+
+// Canonicalise: (min, max), no self loops, sorted, deduplicated.
+static void finish(std::vector<uint64_t> &keys, uint32_t n, kclpp_edge_list *el) {
+  radix_sort_u64(keys);
+  keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+  el->pairs.resize(keys.size() * 2);
+  uint32_t mx = 0;
+  for (size_t i = 0; i < keys.size(); ++i) {
+    uint32_t u = (uint32_t)(keys[i] >> 32), v = (uint32_t)keys[i];
+    el->pairs[2 * i] = u;
+    el->pairs[2 * i + 1] = v;
+    mx = std::max(mx, std::max(u, v));
+  }
+  el->n = keys.empty() ? 1 : mx + 1;
+  (void)n;
+}
+
+static inline uint64_t pack(uint32_t u, uint32_t v) {
+  if (u > v) std::swap(u, v);
+  return ((uint64_t)u << 32) | v;
+}
+
+static std::vector<uint32_t> permutation(uint32_t n, SplitMix &r) {
+  std::vector<uint32_t> p(n);
+  std::iota(p.begin(), p.end(), 0u);
+  for (uint32_t i = n; i > 1; --i) std::swap(p[i - 1], p[r.below(i)]);
+  return p;
+}
+
+static void chung_lu_keys(uint32_t n, double avg, double gamma, SplitMix &r,
+                          const std::vector<uint32_t> &perm, std::vector<uint64_t> &keys) {
+  std::vector<double> w(n);
+  const double ex = -1.0 / (gamma - 1.0);
+  for (uint32_t i = 0; i < n; ++i) w[i] = std::pow((double)(i + 1), ex);
+  Alias al(w);
+  const uint64_t samples = (uint64_t)std::llround((double)n * avg / 2.0);
+  keys.reserve(keys.size() + samples);
+  for (uint64_t i = 0; i < samples; ++i) {
+    uint32_t u = al.draw(r), v = al.draw(r);
+    if (u == v) continue;
+    keys.push_back(pack(perm[u], perm[v]));
+  }
+}
+
+}  // namespace kclpp
+
+using namespace kclpp;
+
+extern "C" {
+
+kclpp_status kclpp_generate(const kclpp_gen_params *p, kclpp_edge_list **out) {
+  if (!p || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_generate: null argument");
+  *out = nullptr;
+  SplitMix rng(p->seed * 0x2545F4914F6CDD1Dull + 0x1234567ull);
+  std::vector<uint64_t> keys;
+  uint32_t n = p->n;
+  try {
+    switch (p->kind) {
+      case KCLPP_GEN_CHUNG_LU: {
+        if (n < 2 || !(p->avg_degree > 0) || !(p->gamma > 1.0))
+          return set_error(KCLPP_ERR_INVALID, "chung-lu: need n >= 2, avg_degree > 0, gamma > 1");
+        auto perm = permutation(n, rng);
+        chung_lu_keys(n, p->avg_degree, p->gamma, rng, perm, keys);
+        break;
+      }
+      case KCLPP_GEN_ER: {
+        if (n < 2 || !(p->avg_degree > 0))
+          return set_error(KCLPP_ERR_INVALID, "er: need n >= 2, avg_degree > 0");
+        const uint64_t samples = (uint64_t)std::llround((double)n * p->avg_degree / 2.0);
+        keys.reserve(samples);
+        for (uint64_t i = 0; i < samples; ++i) {
+          uint32_t u = (uint32_t)rng.below(n), v = (uint32_t)rng.below(n);
+          if (u != v) keys.push_back(pack(u, v));
+        }
+        break;
+      }
+      case KCLPP_GEN_RMAT: {
+        if (p->scale < 1 || p->scale > 31 || p->edge_factor < 1)
+          return set_error(KCLPP_ERR_INVALID, "rmat: need 1 <= scale <= 31, edge_factor >= 1");
+        const double a = p->a, ab = p->a + p->b, abc = p->a + p->b + p->c;
+        if (!(a >= 0 && ab >= a && abc >= ab && abc <= 1.0))
+          return set_error(KCLPP_ERR_INVALID, "rmat: bad quadrant probabilities");
+        n = 1u << p->scale;
+        const uint64_t samples = (uint64_t)p->edge_factor << p->scale;
+        keys.reserve(samples);
+        for (uint64_t i = 0; i < samples; ++i) {
+          uint32_t u = 0, v = 0;
+          for (uint32_t l = 0; l < p->scale; ++l) {
+            double x = rng.uniform();
+            uint32_t bu = 0, bv = 0;
+            if (x < a) { }
+            else if (x < ab) bv = 1;
+            else if (x < abc) bu = 1;
+            else { bu = 1; bv = 1; }
+            u = (u << 1) | bu;
+            v = (v << 1) | bv;
+          }
+          if (u != v) keys.push_back(pack(u, v));
+        }
+        // Scramble ids so that id order carries no degree information.
+        auto perm = permutation(n, rng);
+        for (auto &k : keys) k = pack(perm[(uint32_t)(k >> 32)], perm[(uint32_t)k]);
+        break;
+      }
+      case KCLPP_GEN_PLANTED: {
+        if (n < 2 || !(p->avg_degree > 0) || !(p->gamma > 1.0) || p->comm_min < 2 ||
+            p->comm_max < p->comm_min || !(p->p_in > 0 && p->p_in <= 1.0))
+          return set_error(KCLPP_ERR_INVALID, "planted: bad parameters");
+        auto perm = permutation(n, rng);
+        chung_lu_keys(n, p->avg_degree, p->gamma, rng, perm, keys);
+        // Communities are disjoint slices of a second permutation.
+        auto members = permutation(n, rng);
+        uint64_t at = 0;
+        const double lmin = std::log((double)p->comm_min), lmax = std::log((double)p->comm_max);
+        for (uint32_t c = 0; c < p->communities; ++c) {
+          uint32_t sz = (uint32_t)std::llround(std::exp(lmin + (lmax - lmin) * rng.uniform()));
+          if (at + sz > n) break;
+          for (uint32_t i = 0; i < sz; ++i)
+            for (uint32_t j = i + 1; j < sz; ++j)
+              if (rng.uniform() < p->p_in) keys.push_back(pack(members[at + i], members[at + j]));
+          at += sz;
+        }
+        break;
+      }
+      default:
+        return set_error(KCLPP_ERR_INVALID, "kclpp_generate: unknown kind %d", p->kind);
+    }
+    auto *el = new kclpp_edge_list();
+    finish(keys, n, el);
+    *out = el;
+  } catch (const std::bad_alloc &) {
+    return set_error(KCLPP_ERR_NOMEM, "kclpp_generate: out of host memory");
+  }
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_read_edge_list(const char *path, kclpp_edge_list **out) {
+  if (!path || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_read_edge_list: null argument");
+  *out = nullptr;
+  FILE *f = fopen(path, "r");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s", path);
+  auto *el = new kclpp_edge_list();
+  // A hand-rolled scanner: same accepted grammar as fscanf("%u %u") on
+  // whitespace-separated decimal pairs, several times faster.
+  std::vector<char> buf(1 << 22);
+  uint32_t mx = 0;
+  uint64_t cur = 0;
+  bool innum = false;
+  size_t got;
+  int field = 0;
+  uint32_t first = 0;
+  bool bad = false;
+  while ((got = fread(buf.data(), 1, buf.size(), f)) > 0 && !bad) {
+    for (size_t i = 0; i < got; ++i) {
+      char c = buf[i];
+      if (c >= '0' && c <= '9') {
+        cur = cur * 10 + (uint64_t)(c - '0');
+        if (cur > 0xFFFFFFFFull) { bad = true; break; }
+        innum = true;
+      } else if (c == ' ' || c == '\n' || c == '\t' || c == '\r') {
+        if (innum) {
+          if (field == 0) { first = (uint32_t)cur; field = 1; }
+          else {
+            el->pairs.push_back(first);
+            el->pairs.push_back((uint32_t)cur);
+            mx = std::max(mx, std::max(first, (uint32_t)cur));
+            field = 0;
+          }
+          cur = 0;
+          innum = false;
+        }
+      } else {
+        bad = true;  // fscanf would stop reading here
+        break;
+      }
+    }
+  }
+  if (innum && field == 1 && !bad) {
+    el->pairs.push_back(first);
+    el->pairs.push_back((uint32_t)cur);
+    mx = std::max(mx, std::max(first, (uint32_t)cur));
+  }
+  fclose(f);
+  el->n = mx + 1;
+  *out = el;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_edge_list_create(const uint32_t *pairs, uint64_t e, kclpp_edge_list **out) {
+  if (!out || (!pairs && e)) return set_error(KCLPP_ERR_INVALID, "kclpp_edge_list_create: null argument");
+  auto *el = new kclpp_edge_list();
+  el->pairs.assign(pairs, pairs + 2 * e);
+  uint32_t mx = 0;
+  for (uint32_t v : el->pairs) mx = std::max(mx, v);
+  el->n = mx + 1;
+  *out = el;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_edge_list_info(const kclpp_edge_list *el, uint32_t *n, uint64_t *e) {
+  if (!el) return set_error(KCLPP_ERR_INVALID, "null edge list");
+  if (n) *n = el->n;
+  if (e) *e = el->e();
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_edge_list_copy(const kclpp_edge_list *el, uint32_t *pairs_out) {
+  if (!el || !pairs_out) return set_error(KCLPP_ERR_INVALID, "null argument");
+  if (!el->pairs.empty()) memcpy(pairs_out, el->pairs.data(), el->pairs.size() * sizeof(uint32_t));
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_write_edge_list(const kclpp_edge_list *el, const char *path) {
+  if (!el || !path) return set_error(KCLPP_ERR_INVALID, "null argument");
+  FILE *f = fopen(path, "w");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s for writing", path);
+  std::vector<char> buf;
+  buf.reserve(1 << 22);
+  char tmp[32];
+  for (uint64_t i = 0; i < el->e(); ++i) {
+    int len = snprintf(tmp, sizeof tmp, "%u %u\n", el->pairs[2 * i], el->pairs[2 * i + 1]);
+    buf.insert(buf.end(), tmp, tmp + len);
+    if (buf.size() > (1 << 22) - 64) { fwrite(buf.data(), 1, buf.size(), f); buf.clear(); }
+  }
+  if (!buf.empty()) fwrite(buf.data(), 1, buf.size(), f);
+  int rc = fclose(f);
+  return rc == 0 ? KCLPP_OK : set_error(KCLPP_ERR_IO, "write failed: %s", path);
+}
+
+void kclpp_edge_list_free(kclpp_edge_list *el) { delete el; }
+
+}  // extern "C"

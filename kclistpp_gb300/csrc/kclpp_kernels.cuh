@@ -1,0 +1,741 @@
+// kclpp_kernels.cuh -- the clique kernels (included by one translation unit per mode).
+//
+// Three modes share one root-vertex skeleton (build G_s as bitmaps, then work
+// per row / per root edge):
+//
+//  MODE_COUNT  k-clique degree of every vertex (onepass/recursion,
+//              kClistCoreTrim.c:368-416).  Rows are the symmetric adjacency S
+//              of G_s; the (k-1)-cliques of G_s through x number the
+//              (k-2)-cliques of S[x], counted with the id orientation
+//              A[y] = S[y] ∩ {ids below y}, popcount at the last level.
+//
+//  MODE_ORDER  cliques credited to their smallest-key member (Sim-kClist++'s
+//              rho_add, kCDensestCmpSync.c:138-146; PAVA's largest level,
+//              kCDensestNoAtom.c:191-213).  G_s is relabelled by key rank and
+//              oriented upward: the cliques whose smallest member in G_s is p
+//              number the (k-2)-cliques of Up[p]; p takes them if its key is
+//              below s's, otherwise s does.  Pure popcount counting: no clique
+//              is visited one by one.
+//
+//  MODE_SEQ    Seq-kClist++'s in-place "++" chain (kCDensestNoAtom.c:155-268),
+//              one independent stream per root edge (s, t) starting from the
+//              pass-start r.  Cliques are visited in the reference's order
+//              (ascending ids at every level); the argmin prefix is cached as a
+//              vertex and its value re-read at every comparison, exactly as the
+//              reference does.  At the last level the chain
+//                  for v in V ascending: if cur[v] < cur[g] then cur[v]++ else cur[g]++
+//              runs 32 candidates at a time (tiers M, L): a candidate fails
+//              (credits g) iff cur[v] >= c0 + (failures before it); the failure
+//              mask is the unique fixed point of that rule and is found by
+//              iterating ballots (lane i is final after i+1 rounds, so the loop
+//              is bounded by 33 rounds).
+//
+// Set iteration always walks a copy of the set (`it`) and intersects with the
+// unmodified set, because the child set of u is P ∩ N+(u) over all of P.
+#pragma once
+
+#include "kclpp_dev.cuh"
+
+namespace kclpp {
+namespace dev {
+
+// ========================================================================
+// Tier S: one warp per root, d <= 64, 64-bit rows, one lane per row / edge.
+constexpr int kSMaxD = 64;
+constexpr int kSDl = kSMaxD + 1;  // per-lane delta stride
+
+template <int MODE>
+struct SmemS {
+  uint32_t list[kSMaxD];
+  unsigned long long rows[kSMaxD];
+  unsigned long long base[kSMaxD + 1];  // SEQ: pass-start r; ORDER: keys
+  unsigned long long acc[kSMaxD + 1];   // SEQ: per-root increments
+  uint8_t rank[kSMaxD];
+  uint8_t inv[kSMaxD];
+  uint32_t dl[MODE == MODE_SEQ ? 32 * kSDl : 1];  // SEQ: per-lane stream deltas
+};
+
+__device__ __forceinline__ unsigned long long below64(int y) {
+  return y == 0 ? 0ull : ((1ull << y) - 1ull);
+}
+
+// Number of R-cliques inside P.  Orientation rows[y], restricted to ids below
+// y when BELOW (symmetric rows), used as is otherwise (upward rows).
+template <int R, bool BELOW>
+__device__ __forceinline__ uint64_t cnt64(unsigned long long P, const unsigned long long *rows) {
+  if constexpr (R == 0) {
+    return 1;
+  } else if constexpr (R == 1) {
+    return (uint64_t)__popcll(P);
+  } else {
+    uint64_t c = 0;
+    unsigned long long it = P;
+    while (it) {
+      const int y = __ffsll((long long)it) - 1;
+      it &= it - 1;
+      unsigned long long A = rows[y];
+      if (BELOW) A &= below64(y);
+      c += cnt64<R - 1, BELOW>(P & A, rows);
+    }
+    return c;
+  }
+}
+
+// Seq chain inside one lane (tier S).  L = levels left (k-2 at the top).
+// Returns the number of cliques visited.
+template <int L>
+__device__ __forceinline__ uint32_t seq64(unsigned long long P, int g, const unsigned long long *rows,
+                                          const unsigned long long *base, uint32_t *dl) {
+  if constexpr (L == 1) {
+    // clique_size == 3 branch, kCDensestNoAtom.c:162-171
+    uint32_t c = 0;
+    unsigned long long it = P;
+    while (it) {
+      const int u = __ffsll((long long)it) - 1;
+      it &= it - 1;
+      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
+      dl[g2]++;
+      ++c;
+    }
+    return c;
+  } else if constexpr (L == 2) {
+    // l == 2 branch, kCDensestNoAtom.c:173-188
+    uint32_t c = 0;
+    unsigned long long it = P;
+    while (it) {
+      const int u = __ffsll((long long)it) - 1;
+      it &= it - 1;
+      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
+      unsigned long long V = P & rows[u];
+      while (V) {
+        const int v = __ffsll((long long)V) - 1;
+        V &= V - 1;
+        const int g3 = (base[v] + dl[v]) < (base[g2] + dl[g2]) ? v : g2;
+        dl[g3]++;
+        ++c;
+      }
+    }
+    return c;
+  } else {
+    // general level, kCDensestNoAtom.c:218-267
+    if (__popcll(P) < L) return 0;
+    uint32_t c = 0;
+    unsigned long long it = P;
+    while (it) {
+      const int u = __ffsll((long long)it) - 1;
+      it &= it - 1;
+      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
+      c += seq64<L - 1>(P & rows[u], g2, rows, base, dl);
+    }
+    return c;
+  }
+}
+
+template <int MODE, int K>
+__global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using SM = SmemS<MODE>;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  SM &sm = reinterpret_cast<SM *>(smem_raw)[wid];
+  if constexpr (MODE == MODE_SEQ) {
+    for (int i = lane; i <= kSMaxD; i += 32) sm.acc[i] = 0;
+    for (int i = 0; i < kSDl; ++i) sm.dl[lane * kSDl + i] = 0;
+  }
+  unsigned long long visited = 0;
+  __syncwarp();
+  for (;;) {
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(a.work, 1u);
+    idx = __shfl_sync(KCL_FULL, idx, 0);
+    if (idx >= a.num_roots) break;
+    const uint32_t s = a.roots[idx];
+    const uint64_t o = a.off[s];
+    const int d = (int)(a.off[s + 1] - o);
+    if (d > kSMaxD) {
+      if (lane == 0) atomicOr(a.err, ERR_DEGREE);
+      continue;
+    }
+    if (d < K - 1 || d == 0) continue;
+    for (int i = lane; i < d; i += 32) sm.list[i] = a.cols[o + i];
+    int tau = 0;
+    if constexpr (MODE == MODE_ORDER) {
+      for (int i = lane; i < d; i += 32) sm.base[i] = vertex_key(a, sm.list[i]);
+      const uint64_t ks = vertex_key(a, s);
+      __syncwarp();
+      int t = 0;
+      for (int i = lane; i < d; i += 32) {
+        const uint64_t ki = sm.base[i];
+        int r = 0;
+        for (int j = 0; j < d; ++j) {
+          const uint64_t kj = sm.base[j];
+          r += (kj < ki) || (kj == ki && j < i);
+        }
+        sm.rank[i] = (uint8_t)r;
+        sm.inv[r] = (uint8_t)i;
+        t += (ki <= ks);  // (key_i, i) < (key_s, d): s has the largest id
+      }
+      tau = warp_sum(t);
+    }
+    if constexpr (MODE == MODE_SEQ) {
+      for (int i = lane; i < d; i += 32) sm.base[i] = a.r_in[sm.list[i]];
+      if (lane == 0) sm.base[d] = a.r_in[s];
+    }
+    for (int i = lane; i < kSMaxD; i += 32) sm.rows[i] = 0;
+    __syncwarp();
+    if (K >= 3) {
+      // Row i: out-neighbours of list[i] inside N+(s), by merging the two
+      // ascending lists (MakeSubgraph's induced adjacency, :104-113).
+      for (int i = lane; i < d; i += 32) {
+        const uint32_t x = sm.list[i];
+        const uint64_t xe = a.off[x + 1];
+        unsigned long long row = 0;
+        int j = 0;
+        for (uint64_t e = a.off[x]; e < xe && j < i; ++e) {
+          const uint32_t y = a.cols[e];
+          while (j < i && sm.list[j] < y) ++j;
+          if (j < i && sm.list[j] == y) row |= 1ull << j;
+        }
+        if constexpr (MODE == MODE_SEQ) {
+          sm.rows[i] = row;
+        } else if constexpr (MODE == MODE_COUNT) {
+          atomicOr(&sm.rows[i], row);
+          unsigned long long it = row;
+          while (it) {
+            const int j2 = __ffsll((long long)it) - 1;
+            it &= it - 1;
+            atomicOr(&sm.rows[j2], 1ull << i);
+          }
+        } else {
+          const int ri = sm.rank[i];
+          unsigned long long it = row;
+          while (it) {
+            const int j2 = __ffsll((long long)it) - 1;
+            it &= it - 1;
+            const int rj = sm.rank[j2];
+            const int lo = ri < rj ? ri : rj, hi = ri < rj ? rj : ri;
+            atomicOr(&sm.rows[lo], 1ull << hi);
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if constexpr (MODE == MODE_SEQ) {
+      uint32_t *dl = &sm.dl[lane * kSDl];
+      for (int j = lane; j < d; j += 32) {
+        const unsigned long long C = sm.rows[j];
+        if (!C) continue;
+        const int g0 = sm.base[j] < sm.base[d] ? j : d;  // kCDensestNoAtom.c:287
+        visited += seq64<K - 2>(C, g0, sm.rows, sm.base, dl);
+        // Close the stream: its increments fell on {s, t} ∪ C.
+        unsigned long long it = C;
+        while (it) {
+          const int i = __ffsll((long long)it) - 1;
+          it &= it - 1;
+          if (dl[i]) { atomicAdd(&sm.acc[i], (unsigned long long)dl[i]); dl[i] = 0; }
+        }
+        if (dl[j]) { atomicAdd(&sm.acc[j], (unsigned long long)dl[j]); dl[j] = 0; }
+        if (dl[d]) { atomicAdd(&sm.acc[d], (unsigned long long)dl[d]); dl[d] = 0; }
+      }
+      __syncwarp();
+      for (int i = lane; i <= d; i += 32) {
+        const unsigned long long v = sm.acc[i];
+        if (v) {
+          atomicAdd(&a.out[i < d ? sm.list[i] : s], v);
+          sm.acc[i] = 0;
+        }
+      }
+    } else if constexpr (MODE == MODE_ORDER) {
+      uint64_t ssum = 0;
+      for (int p = lane; p < d; p += 32) {
+        const uint64_t c = cnt64<K - 2, false>(sm.rows[p], sm.rows);
+        if (p < tau) {
+          if (c) atomicAdd(&a.out[sm.list[sm.inv[p]]], (unsigned long long)c);
+        } else {
+          ssum += c;
+        }
+      }
+      ssum = warp_sum(ssum);
+      if (lane == 0 && ssum) atomicAdd(&a.out[s], (unsigned long long)ssum);
+    } else {
+      uint64_t tot = 0;
+      for (int x = lane; x < d; x += 32) {
+        const uint64_t c = cnt64<K - 2, true>(sm.rows[x], sm.rows);
+        if (c) atomicAdd(&a.out[sm.list[x]], (unsigned long long)c);
+        tot += c;
+      }
+      tot = warp_sum(tot);
+      if (lane == 0 && tot) atomicAdd(&a.out[s], (unsigned long long)(tot / (K - 1)));
+    }
+    __syncwarp();
+  }
+  if constexpr (MODE == MODE_SEQ) {
+    if (a.cliques) {
+      visited = warp_sum(visited);
+      if (lane == 0 && visited) atomicAdd(a.cliques, visited);
+    }
+  }
+}
+
+// ========================================================================
+// Tiers M and L: one CTA per root, rows of W 32-bit words, lane w holds word
+// w (tier M, W <= 32) or words w and w + 32 (tier L, W <= 64).
+template <int WPL>
+struct Bits {
+  uint32_t w[WPL];
+};
+
+template <int WPL>
+__device__ __forceinline__ Bits<WPL> load_row(const uint32_t *rows, int r, int W, int lane) {
+  Bits<WPL> b;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    const int w = lane + 32 * q;
+    b.w[q] = w < W ? rows[(size_t)r * W + w] : 0u;
+  }
+  return b;
+}
+template <int WPL>
+__device__ __forceinline__ Bits<WPL> band(const Bits<WPL> &a, const Bits<WPL> &b) {
+  Bits<WPL> c;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) c.w[q] = a.w[q] & b.w[q];
+  return c;
+}
+template <int WPL>
+__device__ __forceinline__ int popc_lane(const Bits<WPL> &a) {
+  int c = 0;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) c += __popc(a.w[q]);
+  return c;
+}
+template <int WPL>
+__device__ __forceinline__ bool any_bits(const Bits<WPL> &a) {
+  uint32_t o = 0;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) o |= a.w[q];
+  return __any_sync(KCL_FULL, o != 0);
+}
+// Mask of the ids below y for this lane's words.
+template <int WPL>
+__device__ __forceinline__ Bits<WPL> below_mask(int y, int lane) {
+  Bits<WPL> b;
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    const int w = lane + 32 * q;
+    const int yw = y >> 5;
+    b.w[q] = w < yw ? 0xffffffffu : (w == yw ? ((1u << (y & 31)) - 1u) : 0u);
+  }
+  return b;
+}
+
+// Visit the members of a distributed set in ascending order (uniform across
+// the warp).  F(u) is called by all lanes.
+template <int WPL, typename F>
+__device__ __forceinline__ void for_each_bit(const Bits<WPL> &P, F &&f) {
+#pragma unroll
+  for (int q = 0; q < WPL; ++q) {
+    uint32_t m = __ballot_sync(KCL_FULL, P.w[q] != 0);
+    while (m) {
+      const int L = __ffs(m) - 1;
+      m &= m - 1;
+      uint32_t wb = __shfl_sync(KCL_FULL, P.w[q], L);
+      while (wb) {
+        const int b = __ffs(wb) - 1;
+        wb &= wb - 1;
+        f((L + 32 * q) * 32 + b);
+      }
+    }
+  }
+}
+
+// Per-lane partial count of R-cliques inside P.
+template <int R, bool BELOW, int WPL>
+__device__ __forceinline__ uint64_t cnt_warp(const Bits<WPL> &P, const uint32_t *rows, int W, int lane) {
+  if constexpr (R == 0) {
+    return lane == 0 ? 1u : 0u;
+  } else if constexpr (R == 1) {
+    return (uint64_t)popc_lane(P);
+  } else {
+    uint64_t c = 0;
+    for_each_bit<WPL>(P, [&](int y) {
+      Bits<WPL> A = load_row<WPL>(rows, y, W, lane);
+      if (BELOW) A = band(A, below_mask<WPL>(y, lane));
+      c += cnt_warp<R - 1, BELOW, WPL>(band(P, A), rows, W, lane);
+    });
+    return c;
+  }
+}
+
+// Shared-memory layout of a tier M / L CTA (dmax = largest out-degree the
+// launch allows, NW warps).  Tier L keeps `rows` in a global slab instead.
+struct LayoutM {
+  size_t list, rows, base, acc, rank, inv, dl, buf, total;
+};
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+__host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, bool rows_in_smem) {
+  LayoutM L;
+  const size_t W = (dmax + 31) / 32;
+  size_t at = 0;
+  L.list = at; at = align16(at + (size_t)dmax * 4);
+  L.rows = at; if (rows_in_smem) at = align16(at + (size_t)dmax * W * 4);
+  L.base = at; if (mode != MODE_COUNT) at = align16(at + (size_t)(dmax + 1) * 8);
+  L.acc = at; if (mode == MODE_SEQ) at = align16(at + (size_t)(dmax + 1) * 8);
+  L.rank = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
+  L.inv = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
+  L.dl = at; if (mode == MODE_SEQ) at = align16(at + (size_t)nw * (dmax + 1) * 4);
+  L.buf = at; if (mode == MODE_SEQ) at = align16(at + (size_t)nw * dmax * 2);
+  L.total = at;
+  return L;
+}
+
+// The Seq chain over V (last level) from prefix argmin g, 32 candidates at a time.
+template <int WPL>
+__device__ __forceinline__ uint32_t chain_warp(const Bits<WPL> &V, int g, const unsigned long long *base,
+                                               uint32_t *dl, uint16_t *buf, int lane, uint32_t *err) {
+  int cntl = popc_lane(V);
+  int incl = cntl;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(KCL_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(KCL_FULL, incl, 31);
+  if (total == 0) return 0;
+  // Ascending order across lanes: lane-major per word group q.  With WPL > 1
+  // the words of lane l are l and l + 32, so order the groups first.
+  if (WPL == 1) {
+    int pos = incl - cntl;
+    uint32_t w = V.w[0];
+    while (w) {
+      const int b = __ffs(w) - 1;
+      w &= w - 1;
+      buf[pos++] = (uint16_t)(lane * 32 + b);
+    }
+  } else {
+    int before = 0;
+#pragma unroll
+    for (int q = 0; q < WPL; ++q) {
+      const int cq = __popc(V.w[q]);
+      int iq = cq;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(KCL_FULL, iq, o);
+        if (lane >= o) iq += t;
+      }
+      int pos = before + iq - cq;
+      uint32_t w = V.w[q];
+      while (w) {
+        const int b = __ffs(w) - 1;
+        w &= w - 1;
+        buf[pos++] = (uint16_t)((lane + 32 * q) * 32 + b);
+      }
+      before += __shfl_sync(KCL_FULL, iq, 31);
+    }
+  }
+  __syncwarp();
+  const unsigned long long c0 = base[g] + dl[g];
+  unsigned long long c = c0;
+  const uint32_t lt = lanemask_lt();
+  for (int b0 = 0; b0 < total; b0 += 32) {
+    const int idx = b0 + lane;
+    const bool valid = idx < total;
+    const int v = valid ? buf[idx] : 0;
+    const unsigned long long av = valid ? base[v] + dl[v] : 0ull;
+    uint32_t m = __ballot_sync(KCL_FULL, valid && av >= c);
+    for (int r = 0; r < 33; ++r) {
+      const uint32_t f = (uint32_t)__popc(m & lt);
+      const uint32_t m2 = __ballot_sync(KCL_FULL, valid && av >= c + f);
+      if (m2 == m) break;
+      m = m2;
+    }
+    if (valid && !((m >> lane) & 1u)) {
+      if (dl[v] == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
+      dl[v] += 1u;
+    }
+    c += (unsigned long long)__popc(m);
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const unsigned long long nd = (unsigned long long)dl[g] + (c - c0);
+    if (nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
+    dl[g] = (uint32_t)nd;
+  }
+  __syncwarp();
+  return (uint32_t)total;
+}
+
+template <int L, int WPL>
+__device__ __forceinline__ uint64_t seq_warp(const Bits<WPL> &P, int g, const uint32_t *rows, int W,
+                                             const unsigned long long *base, uint32_t *dl, uint16_t *buf,
+                                             int lane, uint32_t *err) {
+  if constexpr (L == 1) {
+    return chain_warp<WPL>(P, g, base, dl, buf, lane, err);  // kCDensestNoAtom.c:162-171
+  } else if constexpr (L == 2) {
+    uint64_t c = 0;                                          // kCDensestNoAtom.c:173-188
+    for_each_bit<WPL>(P, [&](int u) {
+      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
+      const Bits<WPL> V = band(P, load_row<WPL>(rows, u, W, lane));
+      c += chain_warp<WPL>(V, g2, base, dl, buf, lane, err);
+    });
+    return c;
+  } else {
+    int pc = warp_sum(popc_lane(P));                          // kCDensestNoAtom.c:218
+    if (pc < L) return 0;
+    uint64_t c = 0;
+    for_each_bit<WPL>(P, [&](int u) {
+      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
+      const Bits<WPL> Q = band(P, load_row<WPL>(rows, u, W, lane));
+      c += seq_warp<L - 1, WPL>(Q, g2, rows, W, base, dl, buf, lane, err);
+    });
+    return c;
+  }
+}
+
+template <int MODE, int K, int WPL, bool ROWS_IN_SMEM>
+__global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NW = kWarpsM;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int dmax = (int)a.dmax;
+  const LayoutM lay = layout_m(MODE, a.dmax, NW, ROWS_IN_SMEM);
+  uint32_t *list = reinterpret_cast<uint32_t *>(smem_raw + lay.list);
+  uint32_t *rows = ROWS_IN_SMEM ? reinterpret_cast<uint32_t *>(smem_raw + lay.rows)
+                                : a.slab + (size_t)blockIdx.x * a.slab_words;
+  unsigned long long *base = reinterpret_cast<unsigned long long *>(smem_raw + lay.base);
+  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem_raw + lay.acc);
+  uint16_t *rank = reinterpret_cast<uint16_t *>(smem_raw + lay.rank);
+  uint16_t *inv = reinterpret_cast<uint16_t *>(smem_raw + lay.inv);
+  uint32_t *dl = reinterpret_cast<uint32_t *>(smem_raw + lay.dl) + (size_t)wid * (dmax + 1);
+  uint16_t *buf = reinterpret_cast<uint16_t *>(smem_raw + lay.buf) + (size_t)wid * dmax;
+
+  __shared__ uint32_t s_idx, s_next;
+  __shared__ int s_tau;
+  __shared__ unsigned long long s_sum;
+
+  if constexpr (MODE == MODE_SEQ) {
+    for (int i = tid; i <= dmax; i += NW * 32) acc[i] = 0;
+    for (int i = lane; i <= dmax; i += 32) dl[i] = 0;
+  }
+  unsigned long long visited = 0;
+  __syncthreads();
+  for (;;) {
+    if (tid == 0) {
+      s_idx = atomicAdd(a.work, 1u);
+      s_next = 0;
+      s_tau = 0;
+      s_sum = 0;
+    }
+    __syncthreads();
+    const uint32_t idx = s_idx;
+    if (idx >= a.num_roots) break;
+    const uint32_t s = a.roots[idx];
+    const uint64_t o = a.off[s];
+    const int d = (int)(a.off[s + 1] - o);
+    if (d > dmax || d > 32 * 32 * WPL) {
+      if (tid == 0) atomicOr(a.err, ERR_DEGREE);
+      __syncthreads();
+      continue;
+    }
+    if (d < K - 1 || d == 0) {
+      __syncthreads();
+      continue;
+    }
+    const int W = (d + 31) >> 5;
+    for (int i = tid; i < d; i += NW * 32) list[i] = a.cols[o + i];
+    for (int i = tid; i < d * W; i += NW * 32) rows[i] = 0;
+    if constexpr (MODE == MODE_ORDER) {
+      for (int i = tid; i < d; i += NW * 32) base[i] = vertex_key(a, a.cols[o + i]);
+      if (tid == 0) base[d] = vertex_key(a, s);
+    }
+    if constexpr (MODE == MODE_SEQ) {
+      for (int i = tid; i < d; i += NW * 32) base[i] = a.r_in[a.cols[o + i]];
+      if (tid == 0) base[d] = a.r_in[s];
+    }
+    __syncthreads();
+    if constexpr (MODE == MODE_ORDER) {
+      const unsigned long long ks = base[d];
+      int t = 0;
+      for (int i = tid; i < d; i += NW * 32) {
+        const unsigned long long ki = base[i];
+        int r = 0;
+        for (int j = 0; j < d; ++j) {
+          const unsigned long long kj = base[j];
+          r += (kj < ki) || (kj == ki && j < i);
+        }
+        rank[i] = (uint16_t)r;
+        inv[r] = (uint16_t)i;
+        t += (ki <= ks);
+      }
+      t = warp_sum(t);
+      if (lane == 0 && t) atomicAdd(&s_tau, t);
+      __syncthreads();
+    }
+    if (K >= 3) {
+      // Row i: N+(list[i]) ∩ N+(s) (MakeSubgraph's induced adjacency,
+      // kCDensestNoAtom.c:104-113), one warp per row, a lane per out-neighbour.
+      for (int i = wid; i < d; i += NW) {
+        if (i == 0) continue;
+        const uint32_t x = list[i];
+        const uint32_t top = list[i - 1];
+        const uint64_t xe = a.off[x + 1];
+        for (uint64_t e = a.off[x] + lane; e < xe; e += 32) {
+          const uint32_t y = a.cols[e];
+          if (y > top) break;  // ascending: no later neighbour is in list[0, i)
+          const int j = lower_bound_u32(list, i, y);
+          if (list[j] != y) continue;
+          if constexpr (MODE == MODE_SEQ) {
+            atomicOr(&rows[(size_t)i * W + (j >> 5)], 1u << (j & 31));
+          } else if constexpr (MODE == MODE_COUNT) {
+            atomicOr(&rows[(size_t)i * W + (j >> 5)], 1u << (j & 31));
+            atomicOr(&rows[(size_t)j * W + (i >> 5)], 1u << (i & 31));
+          } else {
+            const int ri = rank[i], rj = rank[j];
+            const int lo = ri < rj ? ri : rj, hi = ri < rj ? rj : ri;
+            atomicOr(&rows[(size_t)lo * W + (hi >> 5)], 1u << (hi & 31));
+          }
+        }
+      }
+      __syncthreads();
+    }
+    if constexpr (MODE == MODE_SEQ) {
+      for (;;) {
+        int q = 0;
+        if (lane == 0) q = (int)atomicAdd(&s_next, 1u);
+        q = __shfl_sync(KCL_FULL, q, 0);
+        if (q >= d) break;
+        const int j = d - 1 - q;  // larger candidate sets first
+        const Bits<WPL> C = load_row<WPL>(rows, j, W, lane);
+        if (!any_bits<WPL>(C)) continue;
+        const int g0 = base[j] < base[d] ? j : d;  // kCDensestNoAtom.c:287
+        visited += seq_warp<K - 2, WPL>(C, g0, rows, W, base, dl, buf, lane, a.err);
+        // Close the stream: its increments fell on {s, t} ∪ C.
+#pragma unroll
+        for (int qq = 0; qq < WPL; ++qq) {
+          uint32_t w = C.w[qq];
+          while (w) {
+            const int b = __ffs(w) - 1;
+            w &= w - 1;
+            const int i = (lane + 32 * qq) * 32 + b;
+            const uint32_t v = dl[i];
+            if (v) { atomicAdd(&acc[i], (unsigned long long)v); dl[i] = 0; }
+          }
+        }
+        if (lane == 0) {
+          if (dl[j]) { atomicAdd(&acc[j], (unsigned long long)dl[j]); dl[j] = 0; }
+          if (dl[d]) { atomicAdd(&acc[d], (unsigned long long)dl[d]); dl[d] = 0; }
+        }
+        __syncwarp();
+      }
+      __syncthreads();
+      for (int i = tid; i <= d; i += NW * 32) {
+        const unsigned long long v = acc[i];
+        if (v) {
+          atomicAdd(&a.out[i < d ? list[i] : s], v);
+          acc[i] = 0;
+        }
+      }
+    } else {
+      const int tau = (MODE == MODE_ORDER) ? s_tau : 0;
+      unsigned long long mine = 0;
+      for (;;) {
+        int p = 0;
+        if (lane == 0) p = (int)atomicAdd(&s_next, 1u);
+        p = __shfl_sync(KCL_FULL, p, 0);
+        if (p >= d) break;
+        const Bits<WPL> P = load_row<WPL>(rows, p, W, lane);
+        uint64_t c = cnt_warp<K - 2, MODE == MODE_COUNT, WPL>(P, rows, W, lane);
+        c = warp_sum(c);
+        if (lane == 0) {
+          if (MODE == MODE_COUNT) {
+            if (c) atomicAdd(&a.out[list[p]], (unsigned long long)c);
+            mine += c;
+          } else if (p < tau) {
+            if (c) atomicAdd(&a.out[list[inv[p]]], (unsigned long long)c);
+          } else {
+            mine += c;
+          }
+        }
+      }
+      if (lane == 0 && mine) atomicAdd(&s_sum, mine);
+      __syncthreads();
+      if (tid == 0 && s_sum) {
+        const unsigned long long v = (MODE == MODE_COUNT) ? s_sum / (unsigned long long)(K - 1) : s_sum;
+        if (v) atomicAdd(&a.out[s], v);
+      }
+    }
+    __syncthreads();
+  }
+  if constexpr (MODE == MODE_SEQ) {
+    if (a.cliques) {
+      visited = warp_sum(visited);
+      if (lane == 0 && visited) atomicAdd(a.cliques, visited);
+    }
+  }
+}
+
+}  // namespace dev
+
+// Launch one tier of one mode for clique size K.  Persistent grid: as many
+// CTAs as fit on the device at once (bounded by the number of roots).
+template <typename Fn>
+static int persistent_grid(Fn fn, int threads, size_t smem, const TierLaunch &t, int per_cta) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess || nb < 1) nb = 1;
+  long long g = (long long)nb * t.num_sms;
+  const long long need = ((long long)t.num_roots + per_cta - 1) / per_cta;
+  if (need < g) g = need;
+  if (t.max_grid > 0 && g > t.max_grid) g = t.max_grid;
+  return (int)(g < 1 ? 1 : g);
+}
+
+template <int MODE, int K>
+cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
+  using namespace dev;
+  a.roots = t.roots;
+  a.num_roots = t.num_roots;
+  a.dmax = t.dmax;
+  a.work = t.work;
+  if (t.num_roots == 0) return cudaSuccess;
+  if (t.tier == 0) {
+    const size_t sm = sizeof(SmemS<MODE>) * kWarpsS;
+    auto fn = tier_s_kernel<MODE, K>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const int grid = persistent_grid(fn, kWarpsS * 32, sm, t, kWarpsS);
+    fn<<<grid, kWarpsS * 32, sm, st>>>(a);
+    return cudaGetLastError();
+  }
+  if (t.tier == 1) {
+    const size_t sm = layout_m(MODE, t.dmax, kWarpsM, true).total;
+    auto fn = tier_m_kernel<MODE, K, 1, true>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    const int grid = persistent_grid(fn, kWarpsM * 32, sm, t, 1);
+    fn<<<grid, kWarpsM * 32, sm, st>>>(a);
+    return cudaGetLastError();
+  }
+  const size_t sm = layout_m(MODE, t.dmax, kWarpsM, false).total;
+  auto fn = tier_m_kernel<MODE, K, 2, false>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  const int grid = persistent_grid(fn, kWarpsM * 32, sm, t, 1);
+  fn<<<grid, kWarpsM * 32, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int MODE>
+cudaError_t launch_mode(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
+  switch (k) {
+    case 2: if constexpr (MODE == dev::MODE_ORDER) return launch_tier<MODE, 2>(t, a, st); else break;
+    case 3: return launch_tier<MODE, 3>(t, a, st);
+    case 4: return launch_tier<MODE, 4>(t, a, st);
+    case 5: return launch_tier<MODE, 5>(t, a, st);
+    case 6: return launch_tier<MODE, 6>(t, a, st);
+    case 7: return launch_tier<MODE, 7>(t, a, st);
+    case 8: return launch_tier<MODE, 8>(t, a, st);
+    default: break;
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace kclpp

@@ -1,0 +1,125 @@
+// kclpp_order.cpp -- degeneracy order and DAG construction on the host (A2-A4).
+//
+// SortByCore (Graph.c:57-91) is a sequential min-degree peel whose tie order
+// comes from the binary heap of BinaryHeap.c:6-90; the DAG orientation, and
+// with it every clique's enumeration order and every Seq-kClist++ r value,
+// depends on that order.  The heap below performs the same swaps in the same
+// sequence (an implementation of the same algorithm, not a copy), so the rank
+// permutation is identical to the reference's.
+#include <algorithm>
+#include <cstring>
+
+#include "kclpp_internal.h"
+
+namespace kclpp {
+
+namespace {
+struct Heap {
+  // key -> position (UINT32_MAX once popped), position -> (key, value)
+  std::vector<uint32_t> pos;
+  std::vector<uint32_t> key;
+  std::vector<uint64_t> val;
+  uint32_t n = 0;
+  explicit Heap(uint32_t nmax) : pos(nmax, UINT32_MAX), key(nmax), val(nmax) {}
+  inline void swap_at(uint32_t i, uint32_t j) {
+    std::swap(pos[key[i]], pos[key[j]]);
+    std::swap(key[i], key[j]);
+    std::swap(val[i], val[j]);
+  }
+  inline void up(uint32_t i) {
+    while (i > 0) {
+      uint32_t j = (i - 1) >> 1;
+      if (val[j] > val[i]) { swap_at(i, j); i = j; }
+      else break;
+    }
+  }
+  inline void down() {
+    uint32_t i = 0;
+    for (;;) {
+      uint32_t j1 = 2 * i + 1, j2 = j1 + 1;
+      if (j1 >= n) break;
+      uint32_t j = (j2 < n && val[j2] < val[j1]) ? j2 : j1;
+      if (val[j] < val[i]) { swap_at(i, j); i = j; }
+      else break;
+    }
+  }
+  inline void push(uint32_t k, uint64_t v) {
+    pos[k] = n;
+    key[n] = k;
+    val[n] = v;
+    ++n;
+    up(n - 1);
+  }
+  inline void dec(uint32_t k, uint64_t d) {
+    uint32_t i = pos[k];
+    if (i != UINT32_MAX) { val[i] -= d; up(i); }
+  }
+  inline uint32_t pop(uint64_t *v) {
+    uint32_t k = key[0];
+    if (v) *v = val[0];
+    pos[k] = UINT32_MAX;
+    --n;
+    key[0] = key[n];
+    val[0] = val[n];
+    pos[key[0]] = 0;  // as the reference: re-points the last key even when n hits 0
+    down();
+    return k;
+  }
+};
+}  // namespace
+
+void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank) {
+  const uint64_t e = pairs.size() / 2;
+  std::vector<uint64_t> cd((size_t)n + 1, 0);
+  for (uint64_t i = 0; i < e; ++i) { cd[pairs[2 * i] + 1]++; cd[pairs[2 * i + 1] + 1]++; }
+  for (uint32_t i = 1; i <= n; ++i) cd[i] += cd[i - 1];
+  std::vector<uint32_t> adj(2 * e);
+  std::vector<uint64_t> fill(cd.begin(), cd.end() - 1);
+  for (uint64_t i = 0; i < e; ++i) {
+    uint32_t s = pairs[2 * i], t = pairs[2 * i + 1];
+    adj[fill[s]++] = t;
+    adj[fill[t]++] = s;
+  }
+  Heap h(n);
+  for (uint32_t i = 0; i < n; ++i) h.push(i, cd[i + 1] - cd[i]);
+  uint32_t r = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    uint32_t k = h.pop(nullptr);
+    rank[k] = n - (++r);
+    for (uint64_t j = cd[k]; j < cd[k + 1]; ++j) h.dec(adj[j], 1);
+  }
+}
+
+kclpp_status make_dag_host(const std::vector<uint32_t> &pairs, const uint32_t *rank, HostDag &dag) {
+  const uint64_t e = pairs.size() / 2;
+  std::vector<uint64_t> keys(e);
+  uint32_t n = 0;
+  for (uint64_t i = 0; i < e; ++i) {
+    uint32_t s = rank[pairs[2 * i]], t = rank[pairs[2 * i + 1]];
+    if (s < t) std::swap(s, t);
+    if (s == t) return set_error(KCLPP_ERR_INVALID, "edge %llu is a self loop (vertex %u); the graph must be simple",
+                                 (unsigned long long)i, pairs[2 * i]);
+    if (s + 1 > n) n = s + 1;
+    keys[i] = ((uint64_t)s << 32) | t;
+  }
+  radix_sort_u64(keys);  // MakeGraph's qsort by (s, t), Graph.c:125
+  for (uint64_t i = 1; i < e; ++i)
+    if (keys[i] == keys[i - 1])
+      return set_error(KCLPP_ERR_INVALID, "repeated edge in input; the graph must be simple");
+  dag.n = n;
+  dag.off.assign((size_t)n + 1, 0);
+  dag.cols.resize(e);
+  for (uint64_t i = 0; i < e; ++i) {
+    dag.off[(keys[i] >> 32) + 1]++;
+    dag.cols[i] = (uint32_t)keys[i];
+  }
+  uint32_t mx = 0;
+  for (uint32_t i = 1; i <= n; ++i) {
+    mx = std::max<uint32_t>(mx, (uint32_t)dag.off[i]);
+    dag.off[i] += dag.off[i - 1];
+  }
+  dag.core = mx;
+  return KCLPP_OK;
+}
+
+}  // namespace kclpp

@@ -1,0 +1,381 @@
+// kclpp_trim.cpp -- the k-clique core trim (kClistCoreTrim.c), A15-A18.
+//
+// Pipeline (main, kClistCoreTrim.c:707-775):
+//   kcore        degree peel with the reference heap's tie order; vertices whose
+//                running core value is below k-1 are dropped (:242-272)
+//   relabel      survivors renumbered by peel rank, edges oriented high -> low
+//                rank, input order kept (:274-294)
+//   DAG          sorted out-CSR of the survivors (mkspecial, :306-331)
+//   nck          k-clique degree of every survivor: the GPU count kernel on
+//                that DAG (onepass, :394-416)
+//   peel         EXACT: the reference's k-clique-degree heap peel with a local
+//                recount around every popped vertex (kcliquecore/oneshortpass,
+//                :577-666) -- sequential by definition, run on the host;
+//                FAST: GPU rounds that drop every vertex whose k-clique degree
+//                is below the best density seen and recount, ending at the
+//                rho-core for that density
+//   output       trimmed edges in original ids and input order (:686-699)
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "kclpp_internal.h"
+
+using namespace kclpp;
+
+struct kclpp_trim_result {
+  kclpp_trim_info info;
+  std::vector<uint32_t> map;
+  std::vector<uint64_t> nck;
+  std::vector<uint32_t> order;
+  std::vector<uint64_t> core_num;
+  std::vector<uint32_t> trimmed;  // pairs, original ids
+};
+
+namespace {
+
+struct Peel {
+  // indexed min-heap with the reference's operation order (see kclpp_order.cpp)
+  std::vector<uint32_t> pos, key;
+  std::vector<uint64_t> val;
+  uint32_t n = 0;
+  explicit Peel(uint32_t nmax) : pos(nmax, UINT32_MAX), key(nmax), val(nmax) {}
+  void swap_at(uint32_t i, uint32_t j) {
+    std::swap(pos[key[i]], pos[key[j]]);
+    std::swap(key[i], key[j]);
+    std::swap(val[i], val[j]);
+  }
+  void up(uint32_t i) {
+    while (i > 0) {
+      uint32_t j = (i - 1) >> 1;
+      if (val[j] > val[i]) { swap_at(i, j); i = j; }
+      else break;
+    }
+  }
+  void down() {
+    uint32_t i = 0;
+    for (;;) {
+      uint32_t j1 = 2 * i + 1, j2 = j1 + 1;
+      if (j1 >= n) break;
+      uint32_t j = (j2 < n && val[j2] < val[j1]) ? j2 : j1;
+      if (val[j] < val[i]) { swap_at(i, j); i = j; }
+      else break;
+    }
+  }
+  void push(uint32_t k, uint64_t v) { pos[k] = n; key[n] = k; val[n] = v; ++n; up(n - 1); }
+  void dec(uint32_t k, uint64_t d) { uint32_t i = pos[k]; if (i != UINT32_MAX) { val[i] -= d; up(i); } }
+  uint32_t pop(uint64_t *v) {
+    uint32_t k = key[0];
+    *v = val[0];
+    pos[k] = UINT32_MAX;
+    --n;
+    key[0] = key[n]; val[0] = val[n];
+    pos[key[0]] = 0;
+    down();
+    return k;
+  }
+  bool live(uint32_t k) const { return pos[k] != UINT32_MAX; }
+};
+
+inline uint32_t isect(const uint32_t *a, uint32_t na, const uint32_t *b, uint32_t nb, uint32_t *out) {
+  uint32_t i = 0, j = 0, s = 0;
+  while (i < na && j < nb) {
+    if (a[i] < b[j]) ++i;
+    else if (b[j] < a[i]) ++j;
+    else { out[s++] = a[i]; ++i; ++j; }
+  }
+  return s;
+}
+
+// Clique recursion of kClistCoreTrim.c:368-391 over the sorted DAG.
+struct Rec {
+  uint32_t kmax, core;
+  const uint64_t *cd;
+  const uint32_t *adj;
+  std::vector<uint32_t> merge, size, ck;
+  uint64_t *nck;
+  void run(uint32_t k) {
+    const size_t t = (size_t)(k - 3) * core, t2 = t + core;
+    if (size[k - 3] < kmax - k) return;
+    if (k == kmax) {
+      for (uint32_t i = 0; i < kmax - 1; ++i) nck[ck[i]] += size[k - 3];
+      for (uint32_t i = 0; i < size[k - 3]; ++i) nck[merge[t + i]]++;
+      return;
+    }
+    for (uint32_t i = 0; i < size[k - 3]; ++i) {
+      const uint32_t x = merge[t + i];
+      ck[k - 1] = x;
+      size[k - 2] = isect(adj + cd[x], (uint32_t)(cd[x + 1] - cd[x]), &merge[t], size[k - 3], &merge[t2]);
+      run(k + 1);
+    }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int mode, kclpp_trim_result **out) {
+  if (!ctx || !el || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_trim: null argument");
+  *out = nullptr;
+  if (kmax < 3 || kmax > KCLPP_MAX_K)
+    return set_error(KCLPP_ERR_UNSUPPORTED, "k = %d outside [3, %d]", kmax, KCLPP_MAX_K);
+  if (mode != KCLPP_TRIM_EXACT && mode != KCLPP_TRIM_FAST) return set_error(KCLPP_ERR_INVALID, "unknown trim mode");
+  std::unique_ptr<kclpp_trim_result> R(new kclpp_trim_result());
+  kclpp_trim_info &I = R->info;
+  memset(&I, 0, sizeof I);
+  const uint32_t n = el->n;
+  const uint64_t e = el->e();
+  const std::vector<uint32_t> &P = el->pairs;
+  I.n = n;
+  I.e = e;
+  // mkgraph (:198-220)
+  std::vector<uint64_t> cd0((size_t)n + 1, 0);
+  for (uint64_t i = 0; i < e; ++i) { cd0[P[2 * i] + 1]++; cd0[P[2 * i + 1] + 1]++; }
+  for (uint32_t i = 1; i <= n; ++i) cd0[i] += cd0[i - 1];
+  std::vector<uint32_t> adj0(2 * e);
+  {
+    std::vector<uint64_t> f(cd0.begin(), cd0.end() - 1);
+    for (uint64_t i = 0; i < e; ++i) {
+      adj0[f[P[2 * i]]++] = P[2 * i + 1];
+      adj0[f[P[2 * i + 1]]++] = P[2 * i];
+    }
+  }
+  // kcore (:242-272)
+  std::vector<uint32_t> rank(n), map(n);
+  uint32_t n2 = n;
+  {
+    Peel h(n);
+    for (uint32_t i = 0; i < n; ++i) h.push(i, cd0[i + 1] - cd0[i]);
+    uint32_t r = 0, c = 0;
+    const uint32_t kk = (uint32_t)kmax - 1;
+    for (uint32_t i = 0; i < n; ++i) {
+      uint64_t v;
+      uint32_t key = h.pop(&v);
+      if (v > c) c = (uint32_t)v;
+      if (c < kk) { rank[key] = UINT32_MAX; n2--; }
+      else { map[n2 - (++r)] = key; rank[key] = n2 - r; }
+      for (uint64_t j = cd0[key]; j < cd0[key + 1]; ++j) h.dec(adj0[j], 1);
+    }
+    I.core = c;
+  }
+  I.n2 = n2;
+  map.resize(n2);
+  R->map = map;
+  std::vector<uint32_t>().swap(adj0);
+  // relabelnodes (:274-294)
+  std::vector<uint32_t> E;
+  E.reserve(2 * e);
+  for (uint64_t i = 0; i < e; ++i) {
+    uint32_t s = rank[P[2 * i]], t = rank[P[2 * i + 1]];
+    if (s == UINT32_MAX || t == UINT32_MAX) continue;
+    if (s < t) std::swap(s, t);
+    if (s == t) return set_error(KCLPP_ERR_INVALID, "self loop in input; the graph must be simple");
+    E.push_back(s);
+    E.push_back(t);
+  }
+  const uint64_t e2 = E.size() / 2;
+  I.e2 = e2;
+  R->nck.assign(n2, 0);
+  R->order.assign(n2, 0);
+  R->core_num.assign(n2, 0);
+  if (n2 == 0) {
+    *out = R.release();
+    return KCLPP_OK;
+  }
+  // mkspecial (:306-331)
+  std::vector<uint64_t> cd((size_t)n2 + 1, 0);
+  std::vector<uint32_t> adj(e2);
+  {
+    for (uint64_t i = 0; i < e2; ++i) cd[E[2 * i] + 1]++;
+    for (uint32_t i = 1; i <= n2; ++i) cd[i] += cd[i - 1];
+    std::vector<uint64_t> f(cd.begin(), cd.end() - 1);
+    for (uint64_t i = 0; i < e2; ++i) adj[f[E[2 * i]]++] = E[2 * i + 1];
+    for (uint32_t i = 0; i < n2; ++i) std::sort(adj.begin() + cd[i], adj.begin() + cd[i + 1]);
+  }
+  // onepass on the GPU (:394-416)
+  uint64_t tot = 0;
+  {
+    kclpp_graph *g = nullptr;
+    kclpp_status s = kclpp_graph_from_csr(ctx, n2, e2, cd.data(), adj.data(), &g);
+    if (s != KCLPP_OK) return s;
+    s = kclpp_count_cliques(ctx, g, kmax, R->nck.data(), &tot);
+    kclpp_graph_free(g);
+    if (s != KCLPP_OK) return s;
+  }
+  I.total = tot;
+  // mkgraph2 (:547-573)
+  std::vector<uint64_t> cu((size_t)n2 + 1, 0);
+  std::vector<uint32_t> au(2 * e2);
+  {
+    for (uint64_t i = 0; i < e2; ++i) { cu[E[2 * i] + 1]++; cu[E[2 * i + 1] + 1]++; }
+    for (uint32_t i = 1; i <= n2; ++i) cu[i] += cu[i - 1];
+    std::vector<uint64_t> f(cu.begin(), cu.end() - 1);
+    for (uint64_t i = 0; i < e2; ++i) {
+      au[f[E[2 * i]]++] = E[2 * i + 1];
+      au[f[E[2 * i + 1]]++] = E[2 * i];
+    }
+    for (uint32_t i = 0; i < n2; ++i) std::sort(au.begin() + cu[i], au.begin() + cu[i + 1]);
+  }
+  std::vector<char> alive(n2, 0);
+  if (mode == KCLPP_TRIM_EXACT) {
+    // kcliquecore (:605-666)
+    Peel h(n2);
+    for (uint32_t i = 0; i < n2; ++i) h.push(i, R->nck[i]);
+    uint64_t c = 0, ncktot = tot;
+    uint32_t ecount = (uint32_t)e2;  // `unsigned e` in the reference
+    std::vector<uint64_t> whendel((size_t)n2 + 1, 0), nck2((size_t)n2 + 1, 0);
+    std::vector<uint32_t> live((size_t)n2 + 1);
+    I.ncktrim = tot;
+    I.ckrho = (double)ncktot / (double)n2;
+    I.size = n2;
+    I.rho = (double)(2 * ecount) / (double)(n2 * (n2 - 1));
+    Rec rec;
+    rec.kmax = (uint32_t)kmax;
+    rec.core = std::max<uint32_t>(I.core, 1);
+    rec.cd = cd.data();
+    rec.adj = adj.data();
+    rec.merge.assign((size_t)(kmax - 2) * rec.core + 1, 0);
+    rec.size.assign(kmax, 0);
+    rec.ck.assign(kmax, 0);
+    rec.nck = nck2.data();
+    uint32_t i;
+    for (i = 0; i + 1 < n2; ++i) {
+      uint64_t v;
+      const uint32_t u = h.pop(&v);
+      if (v > c) c = v;
+      R->order[i] = u;
+      R->core_num[i] = c;
+      // oneshortpass (:577-603)
+      uint32_t s = 0;
+      for (uint64_t j = cu[u]; j < cu[u + 1]; ++j)
+        if (h.live(au[j])) live[s++] = au[j];
+      if (s > (uint32_t)kmax - 2) {
+        rec.ck[0] = u;
+        for (uint32_t q = 0; q < s; ++q) {
+          const uint32_t w = live[q];
+          rec.ck[1] = w;
+          rec.size[0] = isect(live.data(), s, adj.data() + cd[w], (uint32_t)(cd[w + 1] - cd[w]), rec.merge.data());
+          rec.run(3);
+        }
+      }
+      uint64_t ncktot2 = 0;
+      for (uint64_t j = cu[u]; j < cu[u + 1]; ++j) {
+        const uint32_t w = au[j];
+        if (h.live(w)) {
+          ecount--;
+          h.dec(w, nck2[w]);
+          ncktot2 += nck2[w];
+          nck2[w] = 0;
+        }
+      }
+      const uint32_t size_tmp = n2 - i - 1;
+      whendel[size_tmp] = ncktot2 / (uint64_t)(kmax - 1);
+      ncktot -= whendel[size_tmp];
+      const double ckrho_tmp = (double)ncktot / (double)size_tmp;
+      if (ckrho_tmp > I.ckrho) {
+        I.ckrho = ckrho_tmp;
+        I.size = size_tmp;
+        I.rho = (double)(2 * ecount) / (double)(size_tmp * (size_tmp - 1));
+      }
+    }
+    I.ntrim = n2;  // the reference leaves ntrim unset when n2 == 1
+    for (uint32_t j = n2 - 1; j >= 1; --j) {
+      if ((double)whendel[j] >= I.ckrho) { I.ntrim = j + 1; break; }
+      I.ncktrim -= whendel[j];
+    }
+    uint64_t v;
+    R->order[i] = h.pop(&v);
+    R->core_num[i] = c;
+    I.ckcore = c;
+    for (uint32_t q = n2 - 1; q != n2 - I.ntrim - 1; --q) alive[R->order[q]] = 1;
+  } else {
+    // FAST: density-threshold rounds on the GPU.
+    std::vector<uint64_t> nck = R->nck;
+    std::fill(alive.begin(), alive.end(), 1);
+    uint32_t nl = n2;
+    uint64_t total = tot, el_live = e2;
+    I.ckrho = (double)total / (double)nl;
+    I.size = nl;
+    I.rho = (double)(2 * (uint32_t)el_live) / (double)(nl * (nl - 1));
+    uint32_t removed_at = 0;
+    for (int round = 0; round < 100000; ++round) {
+      std::vector<uint32_t> drop;
+      for (uint32_t v = 0; v < n2; ++v)
+        if (alive[v] && (double)nck[v] < I.ckrho) drop.push_back(v);
+      if (drop.empty()) break;
+      for (uint32_t v : drop) { alive[v] = 0; R->order[removed_at++] = v; }
+      nl -= (uint32_t)drop.size();
+      // live sub-DAG with the same labels
+      std::vector<uint64_t> lcd((size_t)n2 + 1, 0);
+      std::vector<uint32_t> ladj;
+      ladj.reserve(el_live);
+      for (uint32_t s = 0; s < n2; ++s) {
+        if (alive[s])
+          for (uint64_t j = cd[s]; j < cd[s + 1]; ++j)
+            if (alive[adj[j]]) ladj.push_back(adj[j]);
+        lcd[s + 1] = ladj.size();
+      }
+      el_live = ladj.size();
+      std::fill(nck.begin(), nck.end(), 0);
+      total = 0;
+      if (nl) {
+        kclpp_graph *g = nullptr;
+        kclpp_status s = kclpp_graph_from_csr(ctx, n2, el_live, lcd.data(), ladj.data(), &g);
+        if (s != KCLPP_OK) return s;
+        s = kclpp_count_cliques(ctx, g, kmax, nck.data(), &total);
+        kclpp_graph_free(g);
+        if (s != KCLPP_OK) return s;
+        const double dens = (double)total / (double)nl;
+        if (dens > I.ckrho) {
+          I.ckrho = dens;
+          I.size = nl;
+          I.rho = (double)(2 * (uint32_t)el_live) / (double)(nl * (nl - 1));
+        }
+      }
+    }
+    for (uint32_t v = 0; v < n2; ++v)
+      if (alive[v]) R->order[removed_at++] = v;
+    I.ntrim = nl;
+    I.ncktrim = total;
+  }
+  // printdensest trimmed graph (:686-699): input order, original ids.
+  for (uint64_t i = 0; i < e2; ++i) {
+    const uint32_t s = E[2 * i], t = E[2 * i + 1];
+    if (alive[s] && alive[t]) {
+      R->trimmed.push_back(map[s]);
+      R->trimmed.push_back(map[t]);
+    }
+  }
+  I.mtrim = R->trimmed.size() / 2;
+  *out = R.release();
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_trim_info_get(const kclpp_trim_result *t, kclpp_trim_info *info) {
+  if (!t || !info) return set_error(KCLPP_ERR_INVALID, "null argument");
+  *info = t->info;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_trim_copy(const kclpp_trim_result *t, uint32_t *map, uint64_t *nck, uint32_t *order,
+                             uint64_t *core_num) {
+  if (!t) return set_error(KCLPP_ERR_INVALID, "null argument");
+  const size_t n2 = t->info.n2;
+  if (map && n2) memcpy(map, t->map.data(), n2 * 4);
+  if (nck && n2) memcpy(nck, t->nck.data(), n2 * 8);
+  if (order && n2) memcpy(order, t->order.data(), n2 * 4);
+  if (core_num && n2) memcpy(core_num, t->core_num.data(), n2 * 8);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_trim_edges(const kclpp_trim_result *t, kclpp_edge_list **out) {
+  if (!t || !out) return set_error(KCLPP_ERR_INVALID, "null argument");
+  return kclpp_edge_list_create(t->trimmed.data(), t->trimmed.size() / 2, out);
+}
+
+void kclpp_trim_free(kclpp_trim_result *t) { delete t; }
+
+}  // extern "C"

@@ -1,0 +1,124 @@
+/*
+ * kclpp_oracle.h -- CPU restatement of the KClist++ reference algorithms.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker that the GPU path is
+ * compared against (tests/, __graft_entry__.smoke()) and the timed CPU baseline
+ * in bench.py.  Nothing in the shipped library (kclistpp_gb300/) links, loads or
+ * calls it.  Every function names the reference file:line it restates; the
+ * restatement was pinned against the reference programs themselves compiled
+ * from source (oracle/Makefile, target "ref") and against the golden vectors in
+ * tests/golden/.
+ *
+ * Conventions follow the reference: vertex ids are uint32, after orientation an
+ * edge is s->t with s > t, out-lists are ascending.  Counters that the
+ * reference keeps in `unsigned` are widened to 64 bits where the reference's
+ * 32-bit value would wrap only on inputs larger than the reference can read.
+ */
+#ifndef KCLPP_ORACLE_H_
+#define KCLPP_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct { uint32_t s, t; } orc_edge;
+
+/* Directed (degeneracy-oriented) graph, Graph.h:20-27. */
+typedef struct {
+  uint32_t n;        /* number of vertices (max source + 1) */
+  uint64_t e;        /* number of edges */
+  orc_edge *edges;   /* root edges sorted by (s, t) */
+  uint64_t *cd;      /* out-CSR offsets, n + 1 */
+  uint32_t *adj;     /* out-lists, ascending */
+  uint32_t core;     /* max out-degree */
+} orc_graph;
+
+/* Densest-prefix report, kCDensestNoAtom.c:315-320. */
+typedef struct {
+  uint32_t n;
+  uint32_t m;
+  uint64_t cliques;  /* prefix clique count S(n*) (exact numerator of density) */
+  double density;
+  double ub;
+} orc_info;
+
+/* Seq-kClist++ pass orderings. */
+enum {
+  ORC_SEQ_SEQUENTIAL = 0,  /* one chain over all root edges: the reference at p = 1 */
+  ORC_SEQ_EDGE_STREAMS = 1,/* each root edge its own chain from the pass-start r   */
+  ORC_SEQ_THREADS = 2      /* the reference's own p-thread dynamic schedule (timing only) */
+};
+
+/* ---- A1-A4: graph input, degeneracy order, DAG ------------------------- */
+int orc_read_edge_list(const char *path, uint32_t *n, uint64_t *e, orc_edge **edges);
+int orc_write_edge_list(const char *path, uint64_t e, const orc_edge *edges);
+void orc_sort_by_core(uint32_t n, uint64_t e, const orc_edge *edges, uint32_t *rank);
+orc_graph *orc_make_graph(uint32_t n, uint64_t e, const orc_edge *edges, const uint32_t *rank);
+void orc_free_graph(orc_graph *g);
+uint32_t orc_count_edges(const orc_graph *g, uint32_t num_nodes, const uint32_t *nodes);
+
+/* ---- k-clique counts --------------------------------------------------- */
+uint64_t orc_count_cliques(const orc_graph *g, int k, uint64_t *per_vertex /* n or NULL */);
+
+/* ---- Seq-kClist++ (kCDensestNoAtom.c) ---------------------------------- */
+int orc_seq_pass(const orc_graph *g, int k, uint64_t *rho, int mode, int threads);
+void orc_seq_pava(const orc_graph *g, int k, const uint32_t *level, uint64_t *tentative, int threads);
+orc_info orc_seq_find_densest(const orc_graph *g, int k, uint32_t T, const uint64_t *rho,
+                              uint32_t *reordered, uint32_t *level, int threads);
+void orc_sort_by_r_u64(uint32_t n, const uint64_t *rho, uint32_t *reordered);
+/* Sampled pass for the timed CPU baseline: every stride-th root edge; returns cliques visited. */
+uint64_t orc_seq_pass_sample(const orc_graph *g, int k, uint64_t *rho, int mode, int threads, uint64_t stride);
+
+/* ---- Sim-kClist++ (kCDensestCmpSync.c) --------------------------------- */
+void orc_sim_counts(const orc_graph *g, int k, const double *rho, uint64_t *cnt, int threads);
+uint64_t orc_sim_counts_sample(const orc_graph *g, int k, const double *rho, uint64_t *cnt, int threads,
+                               uint64_t stride);
+void orc_sim_update(uint32_t n, uint32_t t, double *rho, const uint64_t *cnt);
+void orc_sim_pava(const orc_graph *g, int k, const uint32_t *level, uint64_t *tentative, int threads);
+orc_info orc_sim_find_densest(const orc_graph *g, int k, const double *rho,
+                              uint32_t *reordered, uint32_t *level, int threads);
+void orc_sort_by_r_f64(uint32_t n, const double *rho, uint32_t *reordered);
+
+/* ---- k-clique core trim (kClistCoreTrim.c) ----------------------------- */
+typedef struct {
+  uint32_t n;            /* vertices in the input edge list (max id + 1) */
+  uint64_t e;            /* input edges */
+  uint32_t n2;           /* vertices with core >= k - 1 */
+  uint64_t e2;           /* edges among them */
+  uint32_t core;         /* degeneracy of the input */
+  uint32_t *map;         /* n2: new label -> original id */
+  uint64_t *nck;         /* n2: k-clique degree per new label */
+  uint64_t total;        /* number of k-cliques */
+  uint32_t *order;       /* n2: peel order, new labels */
+  uint64_t *core_num;    /* n2: k-clique core number along the peel order */
+  uint64_t ckcore;       /* k-clique core number of the graph */
+  double ckrho;          /* best suffix k-clique density */
+  double rho;            /* its edge density */
+  uint32_t size;         /* its size */
+  uint32_t ntrim;        /* vertices kept by the trim */
+  uint64_t ncktrim;      /* k-cliques in the trimmed graph */
+  uint64_t mtrim;        /* edges in the trimmed graph */
+  orc_edge *trimmed;     /* mtrim edges, original ids, in input order */
+} orc_trim_result;
+
+int orc_trim(uint32_t n, uint64_t e, const orc_edge *edges, int k, orc_trim_result *out);
+void orc_free_trim(orc_trim_result *r);
+
+/* ---- whole-program drivers (CDF_Main) ---------------------------------- */
+/* Runs passes 1..2^floor(log2 num_iter) and writes one orc_info per power of two
+ * into infos (capacity max_infos); returns the number of infos written. */
+int orc_seq_main(const orc_graph *g, int k, uint32_t num_iter, int mode, int threads,
+                 uint64_t *rho_out, orc_info *infos, int max_infos);
+int orc_sim_main(const orc_graph *g, int k, uint32_t num_iter, int threads,
+                 double *rho_out, orc_info *infos, int max_infos);
+
+/* ---- timing helper for the CPU baseline -------------------------------- */
+double orc_wtime(void);
+int orc_max_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,119 @@
+"""Host-side logic of the library (no GPU needed): the C ABI's exports, the
+edge-list reader and writer, the seeded generators and the exact degeneracy
+order.  The compute entry points are exercised by the GPU tests."""
+import hashlib
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import kclistpp_gb300 as K
+from oracle import oracle as O
+from tests import golden_util as G
+from tests.conftest import gpu_available
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions() -> list[str]:
+    src = open(os.path.join(ROOT, "include", "kclpp.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(kclpp_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_function():
+    names = declared_functions()
+    assert len(names) >= 40
+    out = subprocess.run(["nm", "-D", "--defined-only", K.LIB_PATH], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (kclpp_\w+)", out))
+    missing = [n for n in names if n not in exported]
+    assert not missing, f"declared but not exported: {missing}"
+    # and the Python binding covers every one of them
+    assert set(names) <= set(K.EXPORTED), set(names) - set(K.EXPORTED)
+
+
+def test_version_and_status_strings():
+    assert "sm_103a" in K.version()
+    for s in range(0, 8):
+        assert K._lib.kclpp_status_string(s)
+
+
+@pytest.mark.skipif(gpu_available(), reason="a GPU is present")
+def test_no_device_is_reported():
+    with pytest.raises(K.KclppError) as ei:
+        K.Context(0)
+    assert ei.value.status == K.ERR_NODEVICE
+
+
+def test_generators_are_deterministic():
+    a = K.chung_lu(3000, 12.0, 2.4, seed=9).pairs()
+    b = K.chung_lu(3000, 12.0, 2.4, seed=9).pairs()
+    c = K.chung_lu(3000, 12.0, 2.4, seed=10).pairs()
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    # canonical form: u < v, sorted, no repeats
+    assert np.all(a[:, 0] < a[:, 1])
+    keys = (a[:, 0].astype(np.uint64) << 32) | a[:, 1]
+    assert np.all(np.diff(keys.astype(np.int64)) > 0)
+
+
+def test_generator_shapes():
+    r = K.rmat(14, 16, seed=2).pairs()
+    assert r.max() < (1 << 14) and 150_000 < len(r) < 16 * (1 << 14)
+    e = K.erdos_renyi(4000, 10.0, seed=1).pairs()
+    assert abs(len(e) - 20000) < 200
+    p = K.planted(5000, 6.0, 2.2, 4, 40, 120, 0.7, seed=3).pairs()
+    assert len(p) > 15000
+
+
+def test_golden_graph_hashes_are_stable():
+    """The generated golden graphs are the ones the reference was run on."""
+    for name in G.index():
+        G.pairs(name)
+
+
+def test_edge_list_roundtrip(tmp_path):
+    P = K.erdos_renyi(500, 8.0, seed=4).pairs()
+    el = K.EdgeList.from_pairs(P)
+    f = tmp_path / "g.txt"
+    el.write(str(f))
+    back = K.read_edge_list(str(f))
+    assert np.array_equal(back.pairs(), P)
+    assert back.n == int(P.max()) + 1
+
+
+def test_read_edge_list_semantics(tmp_path):
+    """ReadEdgeList (Graph.c:34-53): n = max id + 1, reading stops at the first
+    token that is not a number, a trailing half pair is dropped."""
+    f = tmp_path / "a.txt"
+    f.write_text("0 5\n3 2\n\n7 1\n9")
+    el = K.read_edge_list(str(f))
+    assert el.n == 8 and el.e == 3
+    f.write_text("1 2\n2 3\n# comment\n4 5\n")
+    el = K.read_edge_list(str(f))
+    assert el.e == 2
+    f.write_text("")
+    el = K.read_edge_list(str(f))
+    assert el.n == 1 and el.e == 0
+    with pytest.raises(K.KclppError) as ei:
+        K.read_edge_list(str(tmp_path / "missing.txt"))
+    assert ei.value.status == K.ERR_IO
+
+
+@pytest.mark.parametrize("maker", [
+    lambda: K.chung_lu(10000, 20.0, 2.5, seed=1),
+    lambda: K.rmat(13, 16, seed=7),
+    lambda: K.planted(8000, 6.0, 2.1, 3, 50, 150, 0.5, seed=2),
+    lambda: K.EdgeList.from_pairs(G.pairs("kat_clique_tree")),
+])
+def test_core_order_matches_oracle(maker):
+    """SortByCore's rank permutation, including the heap's tie order."""
+    el = maker()
+    assert np.array_equal(K.core_order(el), O.sort_by_core(el.pairs(), el.n))
+
+
+def test_oracle_pins_config1_hash():
+    p = G.pairs("config1_chung_lu_1e4")
+    assert len(p) == 96552
+    assert hashlib.sha256(p.tobytes()).hexdigest() == G.index()["config1_chung_lu_1e4"]["sha256"]

@@ -1,0 +1,82 @@
+"""The CPU oracle against the golden vectors produced by the reference itself.
+
+This pins the oracle: every number below was printed by the reference's own
+functions (kCDensestNoAtom.c, kCDensestCmpSync.c, kClistCoreTrim.c compiled
+from source), and the oracle must reproduce it bit for bit.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import golden_util as G
+
+
+@pytest.mark.parametrize("name,k,T", G.case_ks())
+def test_seq_sequential_matches_reference(name, k, T):
+    """The reference at p = 1 (one in-place chain over all root edges)."""
+    meta = G.index()[name]
+    g = O.Graph(G.pairs(name))
+    assert [g.n, g.m, g.core] == meta["graph"]
+    infos, r = g.seq_main(k, T, mode=O.SEQ_SEQUENTIAL)
+    assert G.infos_equal(meta["runs"][str(k)]["seq_p1"], infos)
+    assert np.array_equal(r, G.arrays(name)[f"k{k}_seq_p1_rho"])
+
+
+@pytest.mark.parametrize("name,k,T", G.case_ks())
+def test_seq_edge_streams_matches_reference(name, k, T):
+    """Per-root-edge streams, run through the reference's own MakeSubgraph and
+    CDF_CliqueEnumThread by the harness."""
+    meta = G.index()[name]
+    g = O.Graph(G.pairs(name))
+    infos, r = g.seq_main(k, T, mode=O.SEQ_EDGE_STREAMS, threads=2)
+    assert G.infos_equal(meta["runs"][str(k)]["seq_edge"], infos)
+    assert np.array_equal(r, G.arrays(name)[f"k{k}_seq_edge_rho"])
+
+
+@pytest.mark.parametrize("name,k,T", G.case_ks())
+def test_sim_matches_reference(name, k, T):
+    """Sim-kClist++: FP64 rho bit-exact, infos bit-exact."""
+    meta = G.index()[name]
+    g = O.Graph(G.pairs(name))
+    infos, rho = g.sim_main(k, T, threads=2)
+    assert G.infos_equal(meta["runs"][str(k)]["sim"], infos)
+    assert np.array_equal(rho.view(np.uint64), G.arrays(name)[f"k{k}_sim_rho_bits"])
+
+
+TRIM_RUNS = [(n, k, T) for (n, k, T) in G.case_ks() if "trim" in G.index()[n]["runs"][str(k)]]
+
+
+@pytest.mark.parametrize("name,k,T", TRIM_RUNS)
+def test_trim_matches_reference(name, k, T):
+    ref = G.index()[name]["runs"][str(k)]["trim"]
+    arr = G.arrays(name)
+    o = O.trim(G.pairs(name), k)
+    deg = arr[f"k{k}_trim_ckdeg"]
+    assert np.array_equal(deg[:, 0], o["map"]) and np.array_equal(deg[:, 1], o["nck"])
+    core = arr[f"k{k}_trim_ckcore"]
+    assert np.array_equal(core[:, 0], o["map"][o["order"]])
+    assert np.array_equal(core[:, 1], o["core_num"])
+    ck = ref["ckdens"]
+    assert ("%f" % o["ckrho"], "%f" % o["rho"], int(ck[2])) == (ck[0], ck[1], o["size"])
+    # printdensest (kClistCoreTrim.c:680) walks i from n-1 while i > n-size-1 in
+    # unsigned arithmetic: when the best suffix is the whole graph the bound
+    # wraps and no vertex is listed.
+    listed = [] if o["size"] == o["n2"] else [str(x) for x in o["map"][o["order"][::-1][: o["size"]]]]
+    assert list(ck[3:]) == listed
+    assert (o["ntrim"], o["mtrim"], o["ncktrim"], o["total"]) == (ref["ntrim"], ref["mtrim"], ref["ncktrim"], ref["total"])
+    assert np.array_equal(arr[f"k{k}_trim_trimmed"].reshape(-1, 2), o["trimmed"])
+
+
+def test_known_answers():
+    """K_10: C(10, k) cliques, densest prefix = the whole clique."""
+    from math import comb
+
+    g = O.Graph(G.pairs("kat_complete10"))
+    for k in range(3, 9):
+        tot, per = g.count_cliques(k)
+        assert tot == comb(10, k)
+        assert np.all(per == comb(9, k - 1))
+        infos, _ = g.seq_main(k, 4)
+        assert infos[-1].n == 10 and infos[-1].cliques == comb(10, k)
+    star = O.Graph(G.pairs("kat_star"))
+    assert star.count_cliques(3)[0] == 0
