@@ -1,0 +1,415 @@
+"""Benchmark: k-cliques/s of the KClist++ "++" pass on one GB300.
+
+Workload (the headline configuration): RMAT scale 20, (a, b, c, d) =
+(0.57, 0.19, 0.19, 0.05), edge factor 16, symmetrised and deduplicated
+(15.7 M edges), k-clique core trimmed at k first; then the degeneracy DAG of
+the trimmed graph.  One step = one Seq-kClist++ pass (per-root-edge streams)
+plus one Sim-kClist++ pass at k (default 4), i.e. every k-clique of the graph
+is processed twice.  Inputs are resident in HBM when the timed region starts;
+the trimmed graph fits in L2, so L2 is flushed (a 256 MiB write) before every
+timed step.
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--k 4]
+
+`--impl reference` times the reference algorithm on the host cores instead:
+the CPU port of kCDensestNoAtom's and kCDensestCmpSync's passes (the oracle,
+with the reference's own p-thread schedule), each step a bounded sample of
+root edges of the same workload.
+
+The graph preparation (generation, trim, DAG) is not timed; the trim counts
+cliques on the GPU in both arms.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-cliques/sec"
+UNIT = "k-cliques/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workload
+def prepare_workload(K, ctx, scale: int, k: int, seed: int, cache_dir: str) -> dict:
+    """RMAT -> FAST k-clique-core trim -> trimmed edge list (cached on disk)."""
+    os.makedirs(cache_dir, exist_ok=True)
+    path = os.path.join(cache_dir, f"rmat{scale}_ef16_s{seed}_k{k}_trim.npz")
+    if os.path.exists(path):
+        z = np.load(path, allow_pickle=False)
+        return {"pairs": z["pairs"], "meta": json.loads(str(z["meta"]))}
+    t0 = time.time()
+    el = K.rmat(scale, 16, 0.57, 0.19, 0.19, seed=seed)
+    tg = time.time() - t0
+    t0 = time.time()
+    tr = K.trim(ctx, el, k, K.TRIM_FAST)
+    tt = time.time() - t0
+    pairs = tr.edges.pairs()
+    i = tr.info
+    meta = dict(rmat_vertices=int(el.n), rmat_edges=int(el.e), k_core_vertices=int(i.n2), k_core_edges=int(i.e2),
+                cliques_before_trim=int(i.total), trimmed_vertices=int(i.ntrim), trimmed_edges=int(i.mtrim),
+                trimmed_cliques=int(i.ncktrim), trim_density=float(i.ckrho), gen_s=round(tg, 2),
+                trim_s=round(tt, 2), trim_mode="fast")
+    tmp = path + ".tmp.npz"
+    np.savez(tmp, pairs=pairs, meta=np.array(json.dumps(meta)))
+    os.replace(tmp, path)
+    return {"pairs": pairs, "meta": meta}
+
+
+def dag_stats(off: np.ndarray, cols: np.ndarray, k: int) -> dict:
+    """Per-root algorithmic bytes by tier (this implementation's minimum) and the
+    per-root-edge figure of the reference's MakeSubgraph (SURVEY formula)."""
+    n = len(off) - 1
+    deg = np.diff(off).astype(np.int64)
+    src = np.repeat(np.arange(n, dtype=np.int64), deg)
+    out_bytes_sum = np.zeros(n, dtype=np.int64)  # Σ_{x∈N+(s)} (16 + 4 d+(x))
+    np.add.at(out_bytes_sum, src, 16 + 4 * deg[cols.astype(np.int64)])
+    per_root = 16 + 4 * deg + out_bytes_sum + 8 * (deg + 1) + 8 * (deg + 1)
+    active = deg >= max(1, k - 1)
+
+    def bucket(d):
+        if d <= 64:
+            return ("S", 0)
+        if d <= 256:
+            return ("M", 256)
+        if d <= 512:
+            return ("M", 512)
+        if d <= 1024:
+            return ("M", 1024)
+        return ("L", 2048)
+
+    tiers = {}
+    for s in np.nonzero(deg > 0)[0]:
+        key = bucket(int(deg[s]))
+        t = tiers.setdefault(key, {"roots": 0, "bytes": 0, "dmax": 0})
+        t["roots"] += 1
+        t["dmax"] = max(t["dmax"], int(deg[s]))
+        if active[s]:
+            t["bytes"] += int(per_root[s])
+    survey = None
+    if n <= 30000:
+        A = np.zeros((n, n), dtype=np.float64)
+        A[src, cols.astype(np.int64)] = 1.0
+        AAt = A @ A.T                      # |N+(s) ∩ N+(t)|
+        ADAt = (A * deg[None, :]) @ A.T    # Σ_{x ∈ C(s,t)} d+(x)
+        e_s, e_t = src, cols.astype(np.int64)
+        C = AAt[e_s, e_t]
+        SD = ADAt[e_s, e_t]
+        survey = int(8 * (n + 1) + np.sum(8 + 4 * (deg[e_s] + deg[e_t]) + 4 * SD + 8 * (C + 2)) + 16 * n)
+    return {"tiers": tiers, "survey_bytes_per_pass": survey, "n": n, "m": int(len(cols))}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        os.unlink(self.file.name)
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                power.append(float(r[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def measured_peaks() -> tuple[float, str]:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle: the reference algorithm ported to a C library)
+def cpu_sample(pairs: np.ndarray, k: int, modes: list[str], seconds: float, threads: int) -> dict:
+    """Time the reference algorithm on a bounded sample of root edges."""
+    from oracle import oracle as O
+
+    og = O.Graph(pairs)
+    r = np.zeros(og.n, dtype=np.uint64)
+    rho = np.zeros(og.n, dtype=np.float64)
+
+    def run(stride):
+        cl, t = 0, 0.0
+        for md in modes:
+            t0 = O.wtime()
+            if md == "seq":
+                cl += og.seq_pass_sample(k, r.copy(), O.SEQ_THREADS, threads, stride)
+            else:
+                cl += og.sim_counts_sample(k, rho, threads, stride)
+            t += O.wtime() - t0
+        return cl, t
+
+    stride = max(1, og.m // 64)
+    cl, t = run(stride)
+    while t < seconds / 8 and stride > 1:
+        stride = max(1, int(stride * max(0.1, t / (seconds / 2))) if t > 0 else stride // 8)
+        cl, t = run(stride)
+    return {"cliques": cl, "seconds": t, "stride": stride, "edges": (og.m + stride - 1) // stride,
+            "m": og.m, "threads": threads}
+
+
+# ---------------------------------------------------------------------------
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--k", type=int, default=4)
+    ap.add_argument("--scale", type=int, default=20)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--modes", default="seq,sim")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "kclpp_bench_cache"))
+    a = ap.parse_args()
+    modes = [m for m in a.modes.split(",") if m]
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if a.impl == "gb300" else "gloo")
+    if a.impl == "reference" and rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    torch.cuda.set_device(local)
+    import kclistpp_gb300 as K
+
+    stream = torch.cuda.current_stream()
+    ctx = K.Context(local, stream=stream.cuda_stream)
+    wl = prepare_workload(K, ctx, a.scale, a.k, a.seed, a.cache)
+    pairs, meta = wl["pairs"], wl["meta"]
+    config = {"workload": f"rmat{a.scale}-ef16 (0.57,0.19,0.19,0.05) k-clique-core-trimmed, k={a.k}; "
+                          f"one step = one {' + one '.join(m.capitalize() + '-kClist++ pass' for m in modes)}",
+              "k": a.k, "graph": meta, "l2": "flushed before every timed step (256 MiB write)",
+              "seq_order": "per-root-edge streams", "parallelism": f"replicas x{world}" if world > 1 else "1 GPU"}
+
+    if a.impl == "reference":
+        threads = os.cpu_count() or 1
+        for _ in range(a.warmup):
+            cpu_sample(pairs, a.k, modes, a.cpu_seconds / 4, threads)
+        res = [cpu_sample(pairs, a.k, modes, a.cpu_seconds, threads) for _ in range(a.steps)]
+        cl = sum(x["cliques"] for x in res)
+        sec = sum(x["seconds"] for x in res)
+        v = cl / sec
+        samp = res[-1]
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": a.warmup, "ms_per_step": 1000 * sec / a.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic", "config": config,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"every {samp['stride']}th root edge ({samp['edges']} of {samp['m']}) "
+                                           f"per mode per step, {', '.join(modes)}; reference p-thread schedule"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        ctx.close()
+        return
+
+    # ---- GB300 arm -----------------------------------------------------------------
+    el = K.EdgeList.from_pairs(pairs)
+    g = K.build_graph(ctx, el)
+    off, cols = g.csr()
+    cliques_per_pass, _ = K.count_cliques(g, a.k)
+    stats = dag_stats(off, cols, a.k)
+    config["dag"] = {"n": g.n, "m": g.m, "max_out_degree": g.core, "cliques_per_pass": int(cliques_per_pass),
+                     "tiers": {f"{t}{d}": v for (t, d), v in stats["tiers"].items()}}
+    n = g.n
+    r_dev = torch.zeros(n, dtype=torch.int64, device="cuda")
+    rho_dev = torch.zeros(n, dtype=torch.float64, device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    t_sim = [1]
+
+    def step():
+        for md in modes:
+            if md == "seq":
+                K.seq_passes_dev(g, a.k, 1, r_dev.data_ptr())
+            else:
+                K.sim_passes_dev(g, a.k, t_sim[0], 1, rho_dev.data_ptr())
+                t_sim[0] += 1
+
+    for _ in range(max(3, a.warmup)):
+        flush.fill_(1)
+        step()
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    ctx.profile(True)
+    ctx.profile_read()
+    launches0 = ctx.launches()
+    evs = []
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall0 = time.perf_counter()
+    for i in range(a.steps):
+        flush.fill_(i & 0xFF)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - wall0
+    launches = ctx.launches() - launches0
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    clk = clocks.stop()
+    ctx.synchronize()
+    step_ms = [x.elapsed_time(y) for x, y in evs]
+    ms = sum(step_ms) / len(step_ms)
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    per_step = cliques_per_pass * len(modes)
+    value = per_step * world / (ms / 1000.0)
+
+    # roofline: the dominant kernel (largest summed time)
+    peak, peak_kind = measured_peaks()
+    dom = max(prof, key=lambda x: x["ms"]) if prof else None
+    roofline = None
+    if dom:
+        key = (dom["tier"], 0 if dom["tier"] == "S" else (2048 if dom["tier"] == "L" else
+               (256 if dom["dmax"] <= 256 else 512 if dom["dmax"] <= 512 else 1024)))
+        bytes_per_launch = stats["tiers"].get(key, {}).get("bytes", 0)
+        avg_ms = dom["ms"] / dom["launches"]
+        achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                    "traffic": None, "kernel": f"{dom['kernel']}-tier{dom['tier']}(dmax {dom['dmax']})",
+                    "bytes_per_launch": bytes_per_launch, "avg_launch_ms": avg_ms,
+                    "peak_source": f"{peak_kind} hbm_gbs",
+                    "note": "bytes = per-root minimum gathers of this kernel; the graph is L2-resident, the "
+                            "kernel is bound by shared-memory/integer issue, not HBM"}
+        if stats["survey_bytes_per_pass"]:
+            roofline["survey_bytes_per_pass"] = stats["survey_bytes_per_pass"]
+    kernels = [{**p, "avg_ms": p["ms"] / max(1, p["launches"])} for p in prof]
+
+    # ---- end to end through the C ABI with host buffers -------------------------------
+    e2e = None
+    if a.e2e_steps > 0:
+        off_h = torch.empty(len(off), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        off_h[:] = off
+        cols_h = torch.empty(len(cols), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+        cols_h[:] = cols
+        r_h = torch.zeros(n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
+        rho_h = torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
+        K.seq_passes_csr(ctx, off_h, cols_h, a.k, 1, r_h)  # warm
+        e2e_t = []
+        tt = 1
+        for _ in range(a.e2e_steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for md in modes:
+                if md == "seq":
+                    K.seq_passes_csr(ctx, off_h, cols_h, a.k, 1, r_h)
+                else:
+                    K.sim_passes_csr(ctx, off_h, cols_h, a.k, 1, rho_h, t_first=tt)
+                    tt += 1
+            e2e_t.append(time.perf_counter() - t0)
+        roots = int(np.count_nonzero(np.diff(off)))
+        graph_bytes = 8 * (n + 1) + 4 * g.m + 4 * g.m + 4 * roots
+        h2d = len(modes) * (graph_bytes + 8 * n)
+        d2h = len(modes) * (8 * n + 4)
+        e2e = {"value": per_step / statistics.median(e2e_t), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": a.e2e_steps,
+               "api": "kclpp_seq_passes_csr / kclpp_sim_passes_csr (host CSR + host r, pinned)"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        threads = os.cpu_count() or 1
+        s = cpu_sample(pairs, a.k, modes, a.cpu_seconds, threads)
+        cpu = {"value": s["cliques"] / s["seconds"], "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"every {s['stride']}th root edge ({s['edges']} of {s['m']}) per mode, "
+                         f"{', '.join(modes)}; {s['seconds']:.1f} s of CPU wall time"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps,
+                "warmup": max(3, a.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic", "config": config,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk, "kernels": kernels, "step_ms": step_ms, "wall_s": wall}
+        print(json.dumps(line), flush=True)
+    g.close()
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

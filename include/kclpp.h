@@ -58,6 +58,24 @@ kclpp_status kclpp_synchronize(kclpp_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 uint64_t kclpp_launch_count(const kclpp_ctx *ctx);
 
+/* Per-kernel timing (no reference counterpart; the reference prints clock()
+ * totals only, kCDensestNoAtom.c:392).  While enabled, every clique-kernel
+ * launch is bracketed by CUDA events on the context's stream.
+ * kclpp_profile_read synchronises, returns one record per (mode, tier) seen
+ * since the previous read, and starts a new period. */
+#define KCLPP_KERNEL_COUNT 0    /* k-clique degrees          */
+#define KCLPP_KERNEL_ORDER 1    /* Sim rho_add / PAVA counts */
+#define KCLPP_KERNEL_SEQ 2      /* Seq "++" chains           */
+typedef struct {
+  int mode;          /* KCLPP_KERNEL_*                         */
+  int tier;          /* 0 = S, 1 = M, 2 = L                    */
+  uint32_t dmax;     /* largest out-degree in the tier         */
+  uint32_t launches;
+  double ms;         /* summed event time                      */
+} kclpp_kernel_time;
+kclpp_status kclpp_profile_enable(kclpp_ctx *ctx, int on);
+kclpp_status kclpp_profile_read(kclpp_ctx *ctx, kclpp_kernel_time *out, int cap, int *count);
+
 /* ---- edge lists (A1) --------------------------------------------------- */
 typedef struct kclpp_edge_list kclpp_edge_list;
 /* ReadEdgeList, Graph.c:34-53: "u v" per line, n = max id + 1. */

@@ -64,6 +64,15 @@ class TrimInfo(C.Structure):
                 ("ntrim", C.c_uint32), ("mtrim", C.c_uint64), ("ncktrim", C.c_uint64)]
 
 
+class KernelTime(C.Structure):
+    _fields_ = [("mode", C.c_int), ("tier", C.c_int), ("dmax", C.c_uint32), ("launches", C.c_uint32),
+                ("ms", C.c_double)]
+
+
+KERNEL_NAMES = {0: "count", 1: "order", 2: "seq"}
+TIER_NAMES = {0: "S", 1: "M", 2: "L"}
+
+
 class GenParams(C.Structure):
     _fields_ = [("kind", C.c_int), ("n", C.c_uint32), ("avg_degree", C.c_double),
                 ("gamma", C.c_double), ("scale", C.c_uint32), ("edge_factor", C.c_uint32),
@@ -93,6 +102,8 @@ _SIGS = {
     "kclpp_destroy": (C.c_int, [_P]),
     "kclpp_synchronize": (C.c_int, [_P]),
     "kclpp_launch_count": (C.c_uint64, [_P]),
+    "kclpp_profile_enable": (C.c_int, [_P, C.c_int]),
+    "kclpp_profile_read": (C.c_int, [_P, C.POINTER(KernelTime), C.c_int, C.POINTER(C.c_int)]),
     "kclpp_read_edge_list": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "kclpp_edge_list_create": (C.c_int, [_u32p, C.c_uint64, C.POINTER(_P)]),
     "kclpp_edge_list_info": (C.c_int, [_P, _u32p, _u64p]),
@@ -172,6 +183,18 @@ class Context:
 
     def launches(self) -> int:
         return int(_lib.kclpp_launch_count(self._h))
+
+    def profile(self, on: bool = True) -> None:
+        _check(_lib.kclpp_profile_enable(self._h, int(on)))
+
+    def profile_read(self) -> list[dict]:
+        """Per-(kernel, tier) launches and summed event time since the last read."""
+        cap = 64
+        buf = (KernelTime * cap)()
+        cnt = C.c_int()
+        _check(_lib.kclpp_profile_read(self._h, buf, cap, C.byref(cnt)))
+        return [dict(kernel=KERNEL_NAMES.get(b.mode, str(b.mode)), tier=TIER_NAMES.get(b.tier, str(b.tier)),
+                     dmax=b.dmax, launches=b.launches, ms=b.ms) for b in buf[: min(cnt.value, cap)]]
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -335,6 +358,16 @@ def seq_passes(g: Graph, k: int, passes: int, r: np.ndarray | None = None,
     r = np.zeros(g.n, dtype=np.uint64) if r is None else np.array(r, dtype=np.uint64, copy=True)
     _check(_lib.kclpp_seq_passes(g.ctx.handle, g._h, k, passes, det_mode, _ptr(r, C.c_uint64)))
     return r
+
+
+def seq_passes_dev(g: Graph, k: int, passes: int, r_ptr: int, det_mode: int = SEQ_EDGE_STREAMS) -> None:
+    """Enqueue `passes` Seq passes on a device r (u64[n] at r_ptr); no synchronisation."""
+    _check(_lib.kclpp_seq_passes_dev(g.ctx.handle, g._h, k, passes, det_mode, _P(r_ptr)))
+
+
+def sim_passes_dev(g: Graph, k: int, t_first: int, passes: int, rho_ptr: int) -> None:
+    """Enqueue Sim passes t_first.. on a device rho (f64[n] at rho_ptr); no synchronisation."""
+    _check(_lib.kclpp_sim_passes_dev(g.ctx.handle, g._h, k, t_first, passes, _P(rho_ptr)))
 
 
 def seq_passes_csr(ctx: Context, offsets, cols, k: int, passes: int, r: np.ndarray,

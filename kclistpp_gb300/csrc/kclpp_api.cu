@@ -36,6 +36,12 @@ using namespace kclpp;
     if (s_ != KCLPP_OK) return s_;         \
   } while (0)
 
+struct PendingTime {
+  int mode, tier;
+  uint32_t dmax;
+  cudaEvent_t a, b;
+};
+
 struct kclpp_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -43,7 +49,21 @@ struct kclpp_ctx {
   int num_sms = 1;
   uint32_t *d_err = nullptr;
   uint64_t launches = 0;
+  bool profile = false;
+  std::vector<PendingTime> pending;
+  std::vector<cudaEvent_t> event_pool;
 };
+
+static cudaEvent_t take_event(kclpp_ctx *c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+  return e;
+}
 
 struct TierInfo {
   int tier;
@@ -236,9 +256,19 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
     cudaError_t e = cudaSuccess;
+    PendingTime pt{mode, t.tier, t.dmax, nullptr, nullptr};
+    if (c->profile) {
+      pt.a = take_event(c);
+      pt.b = take_event(c);
+      if (pt.a) cudaEventRecord(pt.a, c->stream);
+    }
     if (mode == dev::MODE_COUNT) e = launch_count(k, tl, a, c->stream);
     else if (mode == dev::MODE_ORDER) e = launch_order(k, tl, a, c->stream);
     else e = launch_seq(k, tl, a, c->stream);
+    if (c->profile && pt.a && pt.b) {
+      cudaEventRecord(pt.b, c->stream);
+      c->pending.push_back(pt);
+    }
     if (e != cudaSuccess)
       return set_error(KCLPP_ERR_CUDA, "kernel launch (mode %d, tier %d, k %d): %s", mode, t.tier, k,
                        cudaGetErrorString(e));
@@ -363,6 +393,8 @@ kclpp_status kclpp_destroy(kclpp_ctx *c) {
   if (!c) return KCLPP_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+  for (auto e : c->event_pool) cudaEventDestroy(e);
   cudaFree(c->d_err);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -376,6 +408,39 @@ kclpp_status kclpp_synchronize(kclpp_ctx *c) {
 }
 
 uint64_t kclpp_launch_count(const kclpp_ctx *c) { return c ? c->launches : 0; }
+
+kclpp_status kclpp_profile_enable(kclpp_ctx *c, int on) {
+  if (!c) return set_error(KCLPP_ERR_INVALID, "null context");
+  c->profile = on != 0;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_profile_read(kclpp_ctx *c, kclpp_kernel_time *out, int cap, int *count) {
+  if (!c || (!out && cap > 0)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(set_device(c));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  std::vector<kclpp_kernel_time> agg;
+  for (auto &p : c->pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.a, p.b);
+    auto it = std::find_if(agg.begin(), agg.end(), [&](const kclpp_kernel_time &x) {
+      return x.mode == p.mode && x.tier == p.tier && x.dmax == p.dmax;
+    });
+    if (it == agg.end()) {
+      agg.push_back({p.mode, p.tier, p.dmax, 0u, 0.0});
+      it = agg.end() - 1;
+    }
+    it->launches++;
+    it->ms += ms;
+    c->event_pool.push_back(p.a);
+    c->event_pool.push_back(p.b);
+  }
+  c->pending.clear();
+  const int nw = std::min<int>(cap, (int)agg.size());
+  for (int i = 0; i < nw; ++i) out[i] = agg[i];
+  if (count) *count = (int)agg.size();
+  return KCLPP_OK;
+}
 
 // ---- graphs -------------------------------------------------------------------
 kclpp_status kclpp_core_order(const kclpp_edge_list *el, uint32_t *rank_out) {

@@ -458,7 +458,7 @@ uint64_t orc_count_cliques(const orc_graph *g, int k, uint64_t *per_vertex) {
   memset(&p, 0, sizeof p);
   p.kind = 2;
   uint64_t *tmp = per_vertex ? per_vertex : (uint64_t *)xcalloc((size_t)g->n + 1, sizeof(uint64_t));
-  uint64_t c = visit_all(g, k, p, g->n, tmp, 1, 1);
+  uint64_t c = visit_all(g, k, p, g->n, tmp, omp_get_max_threads(), 1);
   if (!per_vertex) free(tmp);
   return c;
 }
