@@ -245,7 +245,11 @@ def main() -> None:
     torch.cuda.set_device(local)
     import kclistpp_gb300 as K
 
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the library launches on it and the timing events are
+    # recorded on it (torch's default stream has the handle 0, which the
+    # library would read as "make your own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = K.Context(local, stream=stream.cuda_stream)
     wl = prepare_workload(K, ctx, a.scale, a.k, a.seed, a.cache)
     pairs, meta = wl["pairs"], wl["meta"]

@@ -83,7 +83,9 @@ struct kclpp_graph {
   unsigned long long *d_a = nullptr, *d_b = nullptr;
   double *d_rho = nullptr;
   uint32_t *d_level = nullptr;
-  uint32_t *d_work = nullptr;
+  uint32_t *d_work = nullptr;   // [0,16): root counters per tier; [16,32): steal cursors
+  uint32_t *d_task = nullptr;   // per-root sub-task counters (tiers M, L)
+  uint32_t num_roots = 0;
   unsigned long long *d_scalar = nullptr;
   uint32_t *d_slab = nullptr;
   uint64_t slab_words = 0;
@@ -193,7 +195,9 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
   KCL_TRY(dalloc(&g->d_roots, all.size()));
   if (!all.empty())
     KCL_CUDA(cudaMemcpyAsync(g->d_roots, all.data(), all.size() * 4, cudaMemcpyHostToDevice, c->stream));
-  KCL_TRY(dalloc(&g->d_work, 16));
+  KCL_TRY(dalloc(&g->d_work, 32));
+  g->num_roots = (uint32_t)all.size();
+  KCL_TRY(dalloc(&g->d_task, all.size()));
   if (!tL.empty()) {
     g->slab_ctas = c->num_sms;
     const uint64_t W = (kTierLMax + 31) / 32;
@@ -233,13 +237,14 @@ static kclpp_status upload_graph(kclpp_ctx *c, kclpp_graph *g) {
 static void free_graph_dev(kclpp_graph *g) {
   cudaFree(g->d_off); cudaFree(g->d_cols); cudaFree(g->d_src); cudaFree(g->d_roots);
   cudaFree(g->d_a); cudaFree(g->d_b); cudaFree(g->d_rho); cudaFree(g->d_level);
-  cudaFree(g->d_work); cudaFree(g->d_scalar); cudaFree(g->d_slab);
+  cudaFree(g->d_work); cudaFree(g->d_task); cudaFree(g->d_scalar); cudaFree(g->d_slab);
 }
 
 // Launch every tier of one mode.
 static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev::PassArgs a) {
   if (g->tiers.empty()) return KCLPP_OK;
-  KCL_CUDA(cudaMemsetAsync(g->d_work, 0, 16 * sizeof(uint32_t), c->stream));
+  KCL_CUDA(cudaMemsetAsync(g->d_work, 0, 32 * sizeof(uint32_t), c->stream));
+  KCL_CUDA(cudaMemsetAsync(g->d_task, 0, (size_t)g->num_roots * sizeof(uint32_t), c->stream));
   a.off = g->d_off;
   a.cols = g->d_cols;
   a.err = c->d_err;
@@ -253,6 +258,8 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     tl.num_roots = t.count;
     tl.dmax = t.dmax;
     tl.work = g->d_work + i;
+    tl.task_next = g->d_task + t.offset;
+    tl.steal_cursor = g->d_work + 16 + i;
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
     cudaError_t e = cudaSuccess;

@@ -13,7 +13,8 @@
 //   tier L  (1024 < d+(s) <= 2048): as tier M with two words per lane and the
 //                                rows in a per-CTA global-memory slab.
 // Roots are taken from a descending-work list by atomic counters (persistent
-// CTAs), root edges / rows inside a root by a shared-memory counter.
+// CTAs); root edges / rows inside a root from a per-root global counter, which
+// CTAs that have run out of roots join (work stealing).
 #pragma once
 
 #include <cstdint>
@@ -40,6 +41,8 @@ struct PassArgs {
   uint32_t num_roots;
   uint32_t dmax;                  // largest out-degree among them
   uint32_t *work;                 // root counter (zeroed before launch)
+  uint32_t *task_next;            // tiers M, L: per-root sub-task counters (zeroed)
+  uint32_t *steal_cursor;         // tiers M, L: first root that may have sub-tasks left
   uint32_t *err;                  // status word
   int key_kind;                   // MODE_ORDER
   const double *rho;              // KEY_SIM
@@ -93,6 +96,8 @@ struct TierLaunch {
   uint32_t num_roots;
   uint32_t dmax;
   uint32_t *work;
+  uint32_t *task_next;
+  uint32_t *steal_cursor;
   int num_sms;
   int max_grid;      // upper bound on CTAs (tier L: CTAs the row slab holds)
 };

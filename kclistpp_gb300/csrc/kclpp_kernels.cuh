@@ -34,6 +34,10 @@
 // unmodified set, because the child set of u is P ∩ N+(u) over all of P.
 #pragma once
 
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "kclpp_dev.cuh"
 
 namespace kclpp {
@@ -491,6 +495,25 @@ __device__ __forceinline__ uint64_t seq_warp(const Bits<WPL> &P, int g, const ui
   }
 }
 
+// Work stealing: once the root list is exhausted, an idle CTA joins a root
+// whose sub-tasks (root edges or rows) are not all taken, rebuilds that root's
+// G_s and takes sub-tasks from the same global counter.  The cursor skips
+// roots known to be exhausted, so the scans cost O(roots) in total.
+constexpr uint32_t kMinSteal = 2;
+__device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
+  uint32_t c = *(volatile uint32_t *)a.steal_cursor;
+  while (c < a.num_roots) {
+    const uint32_t s = a.roots[c];
+    const uint32_t d = (uint32_t)(a.off[s + 1] - a.off[s]);
+    const uint32_t taken = *(volatile uint32_t *)(a.task_next + c);
+    if ((int)d >= need && taken + kMinSteal <= d) return c;
+    atomicMax(a.steal_cursor, c + 1);
+    const uint32_t c2 = *(volatile uint32_t *)a.steal_cursor;
+    c = c2 > c + 1 ? c2 : c + 1;
+  }
+  return UINT32_MAX;
+}
+
 template <int MODE, int K, int WPL, bool ROWS_IN_SMEM>
 __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -508,7 +531,7 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
   uint32_t *dl = reinterpret_cast<uint32_t *>(smem_raw + lay.dl) + (size_t)wid * (dmax + 1);
   uint16_t *buf = reinterpret_cast<uint16_t *>(smem_raw + lay.buf) + (size_t)wid * dmax;
 
-  __shared__ uint32_t s_idx, s_next;
+  __shared__ uint32_t s_idx;
   __shared__ int s_tau;
   __shared__ unsigned long long s_sum;
 
@@ -517,22 +540,29 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
     for (int i = lane; i <= dmax; i += 32) dl[i] = 0;
   }
   unsigned long long visited = 0;
+  bool stealing = false;  // read by thread 0 only
   __syncthreads();
   for (;;) {
     if (tid == 0) {
-      s_idx = atomicAdd(a.work, 1u);
-      s_next = 0;
+      uint32_t idx = UINT32_MAX;
+      if (!stealing) {
+        idx = atomicAdd(a.work, 1u);
+        if (idx >= a.num_roots) stealing = true;
+      }
+      if (stealing) idx = find_victim(a, K - 1);
+      s_idx = idx;
       s_tau = 0;
       s_sum = 0;
     }
     __syncthreads();
     const uint32_t idx = s_idx;
-    if (idx >= a.num_roots) break;
+    if (idx == UINT32_MAX) break;
+    uint32_t *next = a.task_next + idx;  // root's sub-task counter, shared by every CTA on it
     const uint32_t s = a.roots[idx];
     const uint64_t o = a.off[s];
     const int d = (int)(a.off[s + 1] - o);
     if (d > dmax || d > 32 * 32 * WPL) {
-      if (tid == 0) atomicOr(a.err, ERR_DEGREE);
+      if (tid == 0) { atomicOr(a.err, ERR_DEGREE); atomicMax(next, (uint32_t)d); }
       __syncthreads();
       continue;
     }
@@ -600,7 +630,7 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
     if constexpr (MODE == MODE_SEQ) {
       for (;;) {
         int q = 0;
-        if (lane == 0) q = (int)atomicAdd(&s_next, 1u);
+        if (lane == 0) q = (int)atomicAdd(next, 1u);
         q = __shfl_sync(KCL_FULL, q, 0);
         if (q >= d) break;
         const int j = d - 1 - q;  // larger candidate sets first
@@ -639,16 +669,24 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
       unsigned long long mine = 0;
       for (;;) {
         int p = 0;
-        if (lane == 0) p = (int)atomicAdd(&s_next, 1u);
+        if (lane == 0) p = (int)atomicAdd(next, 1u);
         p = __shfl_sync(KCL_FULL, p, 0);
         if (p >= d) break;
         const Bits<WPL> P = load_row<WPL>(rows, p, W, lane);
         uint64_t c = cnt_warp<K - 2, MODE == MODE_COUNT, WPL>(P, rows, W, lane);
         c = warp_sum(c);
+        uint64_t c_low = 0;
+        if constexpr (MODE == MODE_COUNT) {
+          // s's own share: the (k-1)-cliques of G_s whose largest member is p,
+          // i.e. the (k-2)-cliques among p's neighbours below it.  Summing these
+          // (instead of dividing the row total by k-1) stays exact when several
+          // CTAs split one root.
+          c_low = warp_sum(cnt_warp<K - 2, true, WPL>(band(P, below_mask<WPL>(p, lane)), rows, W, lane));
+        }
         if (lane == 0) {
           if (MODE == MODE_COUNT) {
             if (c) atomicAdd(&a.out[list[p]], (unsigned long long)c);
-            mine += c;
+            mine += c_low;
           } else if (p < tau) {
             if (c) atomicAdd(&a.out[list[inv[p]]], (unsigned long long)c);
           } else {
@@ -658,10 +696,7 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
       }
       if (lane == 0 && mine) atomicAdd(&s_sum, mine);
       __syncthreads();
-      if (tid == 0 && s_sum) {
-        const unsigned long long v = (MODE == MODE_COUNT) ? s_sum / (unsigned long long)(K - 1) : s_sum;
-        if (v) atomicAdd(&a.out[s], v);
-      }
+      if (tid == 0 && s_sum) atomicAdd(&a.out[s], s_sum);
     }
     __syncthreads();
   }
@@ -675,15 +710,41 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
 
 }  // namespace dev
 
-// Launch one tier of one mode for clique size K.  Persistent grid: as many
-// CTAs as fit on the device at once (bounded by the number of roots).
+// Per-kernel launch settings, computed once per (kernel, dynamic shared
+// memory size): the opt-in shared-memory attribute and the number of CTAs one
+// SM holds.  Launches then cost no runtime queries.
+struct LaunchCache {
+  std::mutex mu;
+  int attr_bytes = -1;
+  std::vector<std::pair<size_t, int>> occ;  // (smem bytes, CTAs per SM)
+};
+
 template <typename Fn>
-static int persistent_grid(Fn fn, int threads, size_t smem, const TierLaunch &t, int per_cta) {
+static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int *per_sm) {
+  std::lock_guard<std::mutex> g(lc.mu);
+  if ((int)smem > lc.attr_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    lc.attr_bytes = (int)smem;
+  }
+  for (auto &x : lc.occ)
+    if (x.first == smem) { *per_sm = x.second; return cudaSuccess; }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess || nb < 1) nb = 1;
-  long long g = (long long)nb * t.num_sms;
-  const long long need = ((long long)t.num_roots + per_cta - 1) / per_cta;
-  if (need < g) g = need;
+  lc.occ.emplace_back(smem, nb);
+  *per_sm = nb;
+  return cudaSuccess;
+}
+
+// Persistent grid: as many CTAs as are resident at once.  Tier S needs no
+// more warps than roots; tiers M and L keep every resident CTA, because a CTA
+// without a root of its own steals sub-tasks from the unfinished roots.
+static int persistent_grid(int per_sm, const TierLaunch &t, int roots_per_cta, bool steals) {
+  long long g = (long long)per_sm * t.num_sms;
+  if (!steals) {
+    const long long need = ((long long)t.num_roots + roots_per_cta - 1) / roots_per_cta;
+    if (need < g) g = need;
+  }
   if (t.max_grid > 0 && g > t.max_grid) g = t.max_grid;
   return (int)(g < 1 ? 1 : g);
 }
@@ -695,31 +756,34 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
   a.num_roots = t.num_roots;
   a.dmax = t.dmax;
   a.work = t.work;
+  a.task_next = t.task_next;
+  a.steal_cursor = t.steal_cursor;
   if (t.num_roots == 0) return cudaSuccess;
+  int per_sm = 1;
   if (t.tier == 0) {
+    static LaunchCache lc;
     const size_t sm = sizeof(SmemS<MODE>) * kWarpsS;
     auto fn = tier_s_kernel<MODE, K>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = prepare(fn, lc, kWarpsS * 32, sm, &per_sm);
     if (e != cudaSuccess) return e;
-    const int grid = persistent_grid(fn, kWarpsS * 32, sm, t, kWarpsS);
-    fn<<<grid, kWarpsS * 32, sm, st>>>(a);
+    fn<<<persistent_grid(per_sm, t, kWarpsS, false), kWarpsS * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
   if (t.tier == 1) {
+    static LaunchCache lc;
     const size_t sm = layout_m(MODE, t.dmax, kWarpsM, true).total;
     auto fn = tier_m_kernel<MODE, K, 1, true>;
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = prepare(fn, lc, kWarpsM * 32, sm, &per_sm);
     if (e != cudaSuccess) return e;
-    const int grid = persistent_grid(fn, kWarpsM * 32, sm, t, 1);
-    fn<<<grid, kWarpsM * 32, sm, st>>>(a);
+    fn<<<persistent_grid(per_sm, t, 1, true), kWarpsM * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
+  static LaunchCache lc;
   const size_t sm = layout_m(MODE, t.dmax, kWarpsM, false).total;
   auto fn = tier_m_kernel<MODE, K, 2, false>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  cudaError_t e = prepare(fn, lc, kWarpsM * 32, sm, &per_sm);
   if (e != cudaSuccess) return e;
-  const int grid = persistent_grid(fn, kWarpsM * 32, sm, t, 1);
-  fn<<<grid, kWarpsM * 32, sm, st>>>(a);
+  fn<<<persistent_grid(per_sm, t, 1, true), kWarpsM * 32, sm, st>>>(a);
   return cudaGetLastError();
 }
 
