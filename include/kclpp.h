@@ -135,6 +135,23 @@ kclpp_status kclpp_count_edges(kclpp_ctx *ctx, const kclpp_graph *g, uint32_t nu
  * vertex (onepass/recursion, kClistCoreTrim.c:368-416). */
 kclpp_status kclpp_count_cliques(kclpp_ctx *ctx, const kclpp_graph *g, int k,
                                  uint64_t *per_vertex, uint64_t *total);
+/* The same k-clique degrees for callers that cannot allocate device memory
+ * (no counterpart in the reference): code inside a memory pool or arena that
+ * owns the device's memory, pipelines that must not take the allocator's
+ * locks or implicit synchronisation, plug-in hosts that hand over only the
+ * buffers the library may touch.  No context and no allocation: the caller
+ * passes its stream (NULL = the legacy default stream), the DAG as device CSR
+ * (the layout kclpp_graph_copy_csr returns: rows ascending, every column below
+ * its row) and a device output nck_dev[n], which the call clears and fills;
+ * *total (host, optional) receives the number of k-cliques.  The scheduler's
+ * counters live in a static device array of fixed size, so n is limited to
+ * 2,097,152 vertices and out-degrees to 1024 (KCLPP_ERR_UNSUPPORTED beyond).
+ * The first call on a device looks the array's address up: make it before
+ * any stream capture.  Calls share the array, so calls whose kernels overlap
+ * on the GPU race; the call returns after synchronising `stream`. */
+kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, uint64_t m, const uint64_t *offsets_dev,
+                                         const uint32_t *cols_dev, int k, uint64_t *nck_dev,
+                                         uint64_t *total);
 
 /* ---- Seq-kClist++ (A7) --------------------------------------------------- */
 /* Deterministic pass orderings.  EDGE_STREAMS: every root edge runs the

@@ -120,6 +120,7 @@ _SIGS = {
     "kclpp_graph_free": (None, [_P]),
     "kclpp_count_edges": (C.c_int, [_P, _P, C.c_uint32, _u32p, _u32p]),
     "kclpp_count_cliques": (C.c_int, [_P, _P, C.c_int, _u64p, _u64p]),
+    "kclpp_count_cliques_noalloc": (C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, C.c_int, _P, _u64p]),
     "kclpp_seq_passes": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _u64p]),
     "kclpp_seq_passes_dev": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _P]),
     "kclpp_seq_passes_csr": (C.c_int, [_P, C.c_uint32, C.c_uint64, _u64p, _u32p, C.c_int, C.c_uint32,

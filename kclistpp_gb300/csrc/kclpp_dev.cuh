@@ -52,6 +52,8 @@ struct PassArgs {
   unsigned long long *cliques;    // optional: cliques visited (SEQ), nullptr to skip
   uint32_t *slab;                 // tier L: per-CTA row storage in global memory
   uint64_t slab_words;            // words per CTA in slab
+  uint32_t deg_lo, deg_hi;        // id-order schedules: out-degree window of this launch
+  unsigned long long *total;      // id-order schedules: sum of the roots' own clique counts
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {

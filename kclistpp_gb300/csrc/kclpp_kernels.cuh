@@ -135,7 +135,11 @@ __device__ __forceinline__ uint32_t seq64(unsigned long long P, int g, const uns
   }
 }
 
-template <int MODE, int K>
+// IDENT = true: the schedule is every vertex in id order (no root list), a
+// vertex being a root of this launch when its out-degree lies in
+// [a.deg_lo, a.deg_hi]; the roots' own clique counts are also summed into
+// *a.total.  Used by the entry point that allocates nothing.
+template <int MODE, int K, bool IDENT = false>
 __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using SM = SmemS<MODE>;
@@ -152,9 +156,12 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
     if (lane == 0) idx = atomicAdd(a.work, 1u);
     idx = __shfl_sync(KCL_FULL, idx, 0);
     if (idx >= a.num_roots) break;
-    const uint32_t s = a.roots[idx];
+    const uint32_t s = IDENT ? idx : a.roots[idx];
     const uint64_t o = a.off[s];
     const int d = (int)(a.off[s + 1] - o);
+    if constexpr (IDENT) {
+      if ((uint32_t)d < a.deg_lo || (uint32_t)d > a.deg_hi) continue;
+    }
     if (d > kSMaxD) {
       if (lane == 0) atomicOr(a.err, ERR_DEGREE);
       continue;
@@ -268,7 +275,10 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
         tot += c;
       }
       tot = warp_sum(tot);
-      if (lane == 0 && tot) atomicAdd(&a.out[s], (unsigned long long)(tot / (K - 1)));
+      if (lane == 0 && tot) {
+        atomicAdd(&a.out[s], (unsigned long long)(tot / (K - 1)));
+        if constexpr (IDENT) atomicAdd(a.total, (unsigned long long)(tot / (K - 1)));
+      }
     }
     __syncwarp();
   }
@@ -500,13 +510,15 @@ __device__ __forceinline__ uint64_t seq_warp(const Bits<WPL> &P, int g, const ui
 // G_s and takes sub-tasks from the same global counter.  The cursor skips
 // roots known to be exhausted, so the scans cost O(roots) in total.
 constexpr uint32_t kMinSteal = 2;
+template <bool IDENT>
 __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
   uint32_t c = *(volatile uint32_t *)a.steal_cursor;
   while (c < a.num_roots) {
-    const uint32_t s = a.roots[c];
+    const uint32_t s = IDENT ? c : a.roots[c];
     const uint32_t d = (uint32_t)(a.off[s + 1] - a.off[s]);
     const uint32_t taken = *(volatile uint32_t *)(a.task_next + c);
-    if ((int)d >= need && taken + kMinSteal <= d) return c;
+    const bool in_window = !IDENT || (d >= a.deg_lo && d <= a.deg_hi && d <= a.dmax);
+    if (in_window && (int)d >= need && taken + kMinSteal <= d) return c;
     atomicMax(a.steal_cursor, c + 1);
     const uint32_t c2 = *(volatile uint32_t *)a.steal_cursor;
     c = c2 > c + 1 ? c2 : c + 1;
@@ -514,7 +526,7 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
   return UINT32_MAX;
 }
 
-template <int MODE, int K, int WPL, bool ROWS_IN_SMEM>
+template <int MODE, int K, int WPL, bool ROWS_IN_SMEM, bool IDENT = false>
 __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int NW = kWarpsM;
@@ -549,7 +561,7 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
         idx = atomicAdd(a.work, 1u);
         if (idx >= a.num_roots) stealing = true;
       }
-      if (stealing) idx = find_victim(a, K - 1);
+      if (stealing) idx = find_victim<IDENT>(a, K - 1);
       s_idx = idx;
       s_tau = 0;
       s_sum = 0;
@@ -558,9 +570,15 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
     const uint32_t idx = s_idx;
     if (idx == UINT32_MAX) break;
     uint32_t *next = a.task_next + idx;  // root's sub-task counter, shared by every CTA on it
-    const uint32_t s = a.roots[idx];
+    const uint32_t s = IDENT ? idx : a.roots[idx];
     const uint64_t o = a.off[s];
     const int d = (int)(a.off[s + 1] - o);
+    if constexpr (IDENT) {
+      if ((uint32_t)d < a.deg_lo || (uint32_t)d > a.deg_hi) {
+        __syncthreads();
+        continue;
+      }
+    }
     if (d > dmax || d > 32 * 32 * WPL) {
       if (tid == 0) { atomicOr(a.err, ERR_DEGREE); atomicMax(next, (uint32_t)d); }
       __syncthreads();
@@ -696,7 +714,10 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
       }
       if (lane == 0 && mine) atomicAdd(&s_sum, mine);
       __syncthreads();
-      if (tid == 0 && s_sum) atomicAdd(&a.out[s], s_sum);
+      if (tid == 0 && s_sum) {
+        atomicAdd(&a.out[s], s_sum);
+        if constexpr (IDENT && MODE == MODE_COUNT) atomicAdd(a.total, s_sum);
+      }
     }
     __syncthreads();
   }
@@ -716,7 +737,9 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
 struct LaunchCache {
   std::mutex mu;
   int attr_bytes = -1;
-  std::vector<std::pair<size_t, int>> occ;  // (smem bytes, CTAs per SM)
+  size_t occ_smem[32];  // fixed storage: launching never touches the heap
+  int occ_ctas[32];
+  int nocc = 0;
 };
 
 template <typename Fn>
@@ -727,11 +750,15 @@ static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int
     if (e != cudaSuccess) return e;
     lc.attr_bytes = (int)smem;
   }
-  for (auto &x : lc.occ)
-    if (x.first == smem) { *per_sm = x.second; return cudaSuccess; }
+  for (int i = 0; i < lc.nocc; ++i)
+    if (lc.occ_smem[i] == smem) { *per_sm = lc.occ_ctas[i]; return cudaSuccess; }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess || nb < 1) nb = 1;
-  lc.occ.emplace_back(smem, nb);
+  if (lc.nocc < 32) {
+    lc.occ_smem[lc.nocc] = smem;
+    lc.occ_ctas[lc.nocc] = nb;
+    ++lc.nocc;
+  }
   *per_sm = nb;
   return cudaSuccess;
 }
