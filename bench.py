@@ -72,9 +72,11 @@ def prepare_workload(K, ctx, scale: int, k: int, seed: int, cache_dir: str) -> d
     return {"pairs": pairs, "meta": meta}
 
 
-def dag_stats(off: np.ndarray, cols: np.ndarray, k: int) -> dict:
+def dag_stats(off: np.ndarray, cols: np.ndarray, k: int, s_max: int = 64) -> dict:
     """Per-root algorithmic bytes by tier (this implementation's minimum) and the
-    per-root-edge figure of the reference's MakeSubgraph (SURVEY formula)."""
+    per-root-edge figure of the reference's MakeSubgraph (SURVEY formula).
+    s_max is the schedule's tier-S bound (64 for the counting kernels, 16 for
+    the Seq kernel)."""
     n = len(off) - 1
     deg = np.diff(off).astype(np.int64)
     src = np.repeat(np.arange(n, dtype=np.int64), deg)
@@ -84,7 +86,7 @@ def dag_stats(off: np.ndarray, cols: np.ndarray, k: int) -> dict:
     active = deg >= max(1, k - 1)
 
     def bucket(d):
-        if d <= 64:
+        if d <= s_max:
             return ("S", 0)
         if d <= 256:
             return ("M", 256)
@@ -283,9 +285,11 @@ def main() -> None:
     g = K.build_graph(ctx, el)
     off, cols = g.csr()
     cliques_per_pass, _ = K.count_cliques(g, a.k)
-    stats = dag_stats(off, cols, a.k)
+    stats = dag_stats(off, cols, a.k, 64)
+    stats_seq = dag_stats(off, cols, a.k, 16)
     config["dag"] = {"n": g.n, "m": g.m, "max_out_degree": g.core, "cliques_per_pass": int(cliques_per_pass),
-                     "tiers": {f"{t}{d}": v for (t, d), v in stats["tiers"].items()}}
+                     "tiers": {f"{t}{d}": v for (t, d), v in stats["tiers"].items()},
+                     "seq_tiers": {f"{t}{d}": v for (t, d), v in stats_seq["tiers"].items()}}
     n = g.n
     r_dev = torch.zeros(n, dtype=torch.int64, device="cuda")
     rho_dev = torch.zeros(n, dtype=torch.float64, device="cuda")
@@ -351,7 +355,8 @@ def main() -> None:
     if dom:
         key = (dom["tier"], 0 if dom["tier"] == "S" else (2048 if dom["tier"] == "L" else
                (256 if dom["dmax"] <= 256 else 512 if dom["dmax"] <= 512 else 1024)))
-        bytes_per_launch = stats["tiers"].get(key, {}).get("bytes", 0)
+        st = stats_seq if dom["kernel"] == "seq" else stats
+        bytes_per_launch = st["tiers"].get(key, {}).get("bytes", 0)
         avg_ms = dom["ms"] / dom["launches"]
         achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -187,6 +187,27 @@ kclpp_status kclpp_sim_passes_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const 
                                   const uint32_t *cols, int k, uint32_t t_first, uint32_t passes,
                                   double *rho_inout);
 
+/* ---- sharded passes (no reference counterpart) ---------------
+ * A pass splits over devices by root: every rank builds the same graph,
+ * restricts it to its share of roots with kclpp_graph_shard, computes its
+ * part with the *_delta / *_counts entry points below, and the ranks sum the
+ * n-vectors (an all-reduce).  Root edges are independent within a pass, so the
+ * sum equals the unsharded pass exactly (integers). */
+/* owner[v] = rank that processes root v (greedy by out-degree squared). */
+kclpp_status kclpp_shard_plan(uint32_t n, const uint64_t *offsets, uint32_t world, uint32_t *owner);
+/* Restrict g's root schedule to `rank`'s share (world = 1 restores all roots). */
+kclpp_status kclpp_graph_shard(kclpp_ctx *ctx, kclpp_graph *g, uint32_t rank, uint32_t world);
+/* Seq pass increments of g's roots from r (device): delta = r_after - r, for
+ * this shard only (CDF_CliqueEnum FRANK_WOLFE, kCDensestNoAtom.c:270-295). */
+kclpp_status kclpp_seq_delta_dev(kclpp_ctx *ctx, const kclpp_graph *g, int k, const uint64_t *r_dev,
+                                 uint64_t *delta_dev);
+/* Sim rho_add of g's roots (device), and the rho update on a summed rho_add
+ * (kCDensestCmpSync.c:298-325, 402-403). */
+kclpp_status kclpp_sim_counts_dev(kclpp_ctx *ctx, const kclpp_graph *g, int k, const double *rho_dev,
+                                  uint64_t *cnt_dev);
+kclpp_status kclpp_sim_update_dev(kclpp_ctx *ctx, uint32_t n, uint32_t t, double *rho_dev,
+                                  const uint64_t *cnt_dev);
+
 /* ---- sort by r, PAVA pass, densest prefix (A10-A13) ------------------------ */
 /* CDF_NodeCmp + qsort (kCDensestNoAtom.c:322-337): vertices by r descending,
  * ties by ascending id; level[reordered[i]] = i.  Either output may be NULL. */

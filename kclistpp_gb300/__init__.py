@@ -83,7 +83,7 @@ class GenParams(C.Structure):
 
 def _load() -> C.CDLL:
     if not os.path.exists(LIB_PATH):
-        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m kclistpp_gb300.build`")
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python kclistpp_gb300/build.py`")
     return C.CDLL(LIB_PATH)
 
 
@@ -130,6 +130,11 @@ _SIGS = {
     "kclpp_sim_passes_dev": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_uint32, _P]),
     "kclpp_sim_passes_csr": (C.c_int, [_P, C.c_uint32, C.c_uint64, _u64p, _u32p, C.c_int, C.c_uint32,
                                        C.c_uint32, _f64p]),
+    "kclpp_shard_plan": (C.c_int, [C.c_uint32, _u64p, C.c_uint32, _u32p]),
+    "kclpp_graph_shard": (C.c_int, [_P, _P, C.c_uint32, C.c_uint32]),
+    "kclpp_seq_delta_dev": (C.c_int, [_P, _P, C.c_int, _P, _P]),
+    "kclpp_sim_counts_dev": (C.c_int, [_P, _P, C.c_int, _P, _P]),
+    "kclpp_sim_update_dev": (C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P]),
     "kclpp_sort_by_r_u64": (C.c_int, [_P, C.c_uint32, _u64p, _u32p, _u32p]),
     "kclpp_sort_by_r_f64": (C.c_int, [_P, C.c_uint32, _f64p, _u32p, _u32p]),
     "kclpp_pava": (C.c_int, [_P, _P, C.c_int, _u32p, _u64p]),
@@ -376,6 +381,31 @@ def seq_passes_csr(ctx: Context, offsets, cols, k: int, passes: int, r: np.ndarr
     """One-shot host call (upload DAG + passes + download); r is updated in place."""
     _check(_lib.kclpp_seq_passes_csr(ctx.handle, len(offsets) - 1, len(cols), _ptr(offsets, C.c_uint64),
                                      _ptr(cols, C.c_uint32), k, passes, det_mode, _ptr(r, C.c_uint64)))
+
+
+def shard_plan(offsets: np.ndarray, world: int) -> np.ndarray:
+    """owner[v]: the rank that processes root v when a pass is split over `world` devices."""
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    n = len(off) - 1
+    owner = np.empty(max(n, 1), dtype=np.uint32)
+    _check(_lib.kclpp_shard_plan(n, _ptr(off, C.c_uint64), world, _ptr(owner, C.c_uint32)))
+    return owner[:n]
+
+
+def graph_shard(g: Graph, rank: int, world: int) -> None:
+    _check(_lib.kclpp_graph_shard(g.ctx.handle, g._h, rank, world))
+
+
+def seq_delta_dev(g: Graph, k: int, r_ptr: int, delta_ptr: int) -> None:
+    _check(_lib.kclpp_seq_delta_dev(g.ctx.handle, g._h, k, _P(r_ptr), _P(delta_ptr)))
+
+
+def sim_counts_dev(g: Graph, k: int, rho_ptr: int, cnt_ptr: int) -> None:
+    _check(_lib.kclpp_sim_counts_dev(g.ctx.handle, g._h, k, _P(rho_ptr), _P(cnt_ptr)))
+
+
+def sim_update_dev(ctx: Context, n: int, t: int, rho_ptr: int, cnt_ptr: int) -> None:
+    _check(_lib.kclpp_sim_update_dev(ctx.handle, n, t, _P(rho_ptr), _P(cnt_ptr)))
 
 
 def sim_counts(g: Graph, k: int, rho: np.ndarray) -> np.ndarray:

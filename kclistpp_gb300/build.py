@@ -1,7 +1,7 @@
 """Builds libkclpp.so (CUDA kernels for sm_103a + the C ABI) in-tree.
 
-    python -m kclistpp_gb300.build            # library + drop-in programs
-    python -m kclistpp_gb300.build --force    # rebuild everything
+    python kclistpp_gb300/build.py            # library + drop-in programs
+    python kclistpp_gb300/build.py --force    # rebuild everything
 
 Translation units compile in parallel; objects go to kclistpp_gb300/_build/,
 the library to kclistpp_gb300/libkclpp.so and the drop-in command-line

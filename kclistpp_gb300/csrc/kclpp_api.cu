@@ -77,7 +77,13 @@ struct kclpp_graph {
   uint32_t *d_cols = nullptr;
   uint32_t *d_src = nullptr;
   uint32_t *d_roots = nullptr;
-  std::vector<TierInfo> tiers;
+  // Two schedules over the same roots: [0] for the counting kernels (tier S up
+  // to out-degree 64), [1] for the Seq kernel (tier S up to 16).
+  std::vector<TierInfo> tiers[2];
+  // Sharding (several devices splitting one pass): owner rank of every root.
+  std::vector<uint32_t> owner;
+  uint32_t shard_rank = 0, shard_world = 1;
+  uint32_t sched_base[2] = {0, 0};
   uint32_t maxdeg = 0;
   // workspace
   unsigned long long *d_a = nullptr, *d_b = nullptr;
@@ -151,54 +157,82 @@ static kclpp_status dalloc(T **p, size_t count) {
   return KCLPP_OK;
 }
 
-// Root schedule: tiers by out-degree, descending work (out-degree squared,
-// then id) inside each tier.
+// Root partition for sharded passes: roots by descending estimated work
+// (out-degree squared), each to the rank with the least work so far (ties to
+// the lower rank).  Deterministic, so every rank computes the same plan.
+static void shard_plan_host(uint32_t n, const uint64_t *off, uint32_t world, uint32_t *owner) {
+  std::vector<uint32_t> roots;
+  for (uint32_t s = 0; s < n; ++s) {
+    owner[s] = 0;
+    if (off[s + 1] > off[s]) roots.push_back(s);
+  }
+  auto w = [&](uint32_t s) { const uint64_t d = off[s + 1] - off[s]; return d * d; };
+  std::stable_sort(roots.begin(), roots.end(), [&](uint32_t a, uint32_t b) { return w(a) > w(b); });
+  std::vector<uint64_t> load(world, 0);
+  for (uint32_t s : roots) {
+    uint32_t best = 0;
+    for (uint32_t r = 1; r < world; ++r)
+      if (load[r] < load[best]) best = r;
+    owner[s] = best;
+    load[best] += w(s);
+  }
+}
+
+// Root schedules: tiers by out-degree, descending work (out-degree, then id)
+// inside each tier; tier L first, then tier M from the largest roots down, so
+// that the longest CTAs start first.
 static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
   const HostDag &D = g->dag;
-  std::vector<uint32_t> tS, tM1, tM2, tM3, tL;
-  uint32_t mx = 0;
-  for (uint32_t s = 0; s < D.n; ++s) {
-    const uint32_t d = (uint32_t)(D.off[s + 1] - D.off[s]);
-    if (d == 0) continue;
-    mx = std::max(mx, d);
-    if (d <= kTierSMax) tS.push_back(s);
-    else if (d <= 256) tM1.push_back(s);
-    else if (d <= 512) tM2.push_back(s);
-    else if (d <= kTierMMax) tM3.push_back(s);
-    else tL.push_back(s);
-  }
-  g->maxdeg = mx;
   auto deg = [&](uint32_t s) { return (uint32_t)(D.off[s + 1] - D.off[s]); };
   auto by_work = [&](uint32_t a, uint32_t b) {
     const uint32_t da = deg(a), db = deg(b);
     return da != db ? da > db : a < b;
   };
   std::vector<uint32_t> all;
-  g->tiers.clear();
-  auto add = [&](std::vector<uint32_t> &v, int tier) {
-    if (v.empty()) return;
-    std::sort(v.begin(), v.end(), by_work);
-    TierInfo t;
-    t.tier = tier;
-    t.offset = (uint32_t)all.size();
-    t.count = (uint32_t)v.size();
-    t.dmax = deg(v.front());
-    all.insert(all.end(), v.begin(), v.end());
-    g->tiers.push_back(t);
-  };
-  // Largest roots first so that their long CTAs start early.
-  add(tL, 2);
-  add(tM3, 1);
-  add(tM2, 1);
-  add(tM1, 1);
-  add(tS, 0);
+  bool any_l = false;
+  uint32_t mx = 0;
+  for (int sch = 0; sch < 2; ++sch) {
+    const uint32_t smax = sch == 0 ? kTierSMax : kTierSMaxSeq;
+    std::vector<uint32_t> tS, tM1, tM2, tM3, tL;
+    for (uint32_t s = 0; s < D.n; ++s) {
+      const uint32_t d = deg(s);
+      if (d == 0) continue;
+      if (g->shard_world > 1 && g->owner[s] != g->shard_rank) continue;
+      mx = std::max(mx, d);
+      if (d <= smax) tS.push_back(s);
+      else if (d <= 256) tM1.push_back(s);
+      else if (d <= 512) tM2.push_back(s);
+      else if (d <= kTierMMax) tM3.push_back(s);
+      else tL.push_back(s);
+    }
+    any_l |= !tL.empty();
+    g->sched_base[sch] = (uint32_t)all.size();
+    g->tiers[sch].clear();
+    auto add = [&](std::vector<uint32_t> &v, int tier) {
+      if (v.empty()) return;
+      std::sort(v.begin(), v.end(), by_work);
+      TierInfo t;
+      t.tier = tier;
+      t.offset = (uint32_t)all.size();
+      t.count = (uint32_t)v.size();
+      t.dmax = deg(v.front());
+      all.insert(all.end(), v.begin(), v.end());
+      g->tiers[sch].push_back(t);
+    };
+    add(tL, 2);
+    add(tM3, 1);
+    add(tM2, 1);
+    add(tM1, 1);
+    add(tS, 0);
+    if (sch == 0) g->num_roots = (uint32_t)all.size();
+  }
+  g->maxdeg = mx;
   KCL_TRY(dalloc(&g->d_roots, all.size()));
   if (!all.empty())
     KCL_CUDA(cudaMemcpyAsync(g->d_roots, all.data(), all.size() * 4, cudaMemcpyHostToDevice, c->stream));
   KCL_TRY(dalloc(&g->d_work, 32));
-  g->num_roots = (uint32_t)all.size();
-  KCL_TRY(dalloc(&g->d_task, all.size()));
-  if (!tL.empty()) {
+  KCL_TRY(dalloc(&g->d_task, g->num_roots));
+  if (any_l) {
     g->slab_ctas = c->num_sms;
     const uint64_t W = (kTierLMax + 31) / 32;
     g->slab_words = (uint64_t)kTierLMax * W;
@@ -242,7 +276,9 @@ static void free_graph_dev(kclpp_graph *g) {
 
 // Launch every tier of one mode.
 static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev::PassArgs a) {
-  if (g->tiers.empty()) return KCLPP_OK;
+  const int sch = mode == dev::MODE_SEQ ? 1 : 0;
+  const std::vector<TierInfo> &tiers = g->tiers[sch];
+  if (tiers.empty()) return KCLPP_OK;
   KCL_CUDA(cudaMemsetAsync(g->d_work, 0, 32 * sizeof(uint32_t), c->stream));
   KCL_CUDA(cudaMemsetAsync(g->d_task, 0, (size_t)g->num_roots * sizeof(uint32_t), c->stream));
   a.off = g->d_off;
@@ -250,16 +286,18 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
   a.err = c->d_err;
   a.slab = g->d_slab;
   a.slab_words = g->slab_words;
-  for (size_t i = 0; i < g->tiers.size(); ++i) {
-    const TierInfo &t = g->tiers[i];
+  for (size_t i = 0; i < tiers.size(); ++i) {
+    const TierInfo &t = tiers[i];
     TierLaunch tl;
     tl.tier = t.tier;
     tl.roots = g->d_roots + t.offset;
     tl.num_roots = t.count;
     tl.dmax = t.dmax;
     tl.work = g->d_work + i;
-    tl.task_next = g->d_task + t.offset;
-    tl.steal_cursor = g->d_work + 16 + i;
+    tl.task_next = g->d_task + (t.offset - g->sched_base[sch]);
+    // Work stealing pays off for the Seq chains (long, uneven root edges); the
+    // counting kernels finish their roots quickly and do not steal.
+    tl.steal_cursor = mode == dev::MODE_SEQ ? g->d_work + 16 + i : nullptr;
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
     cudaError_t e = cudaSuccess;
@@ -646,6 +684,59 @@ kclpp_status kclpp_sim_passes_csr(kclpp_ctx *c, uint32_t n, uint64_t m, const ui
   kclpp_status s = kclpp_sim_passes(c, g, k, t_first, passes, rho);
   kclpp_graph_free(g);
   return s;
+}
+
+// ---- sharded passes (several devices splitting one pass) -----------------------------
+kclpp_status kclpp_shard_plan(uint32_t n, const uint64_t *offsets, uint32_t world, uint32_t *owner) {
+  if (!offsets || (!owner && n) || world == 0) return set_error(KCLPP_ERR_INVALID, "kclpp_shard_plan: bad argument");
+  shard_plan_host(n, offsets, world, owner);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_graph_shard(kclpp_ctx *c, kclpp_graph *g, uint32_t rank, uint32_t world) {
+  if (!c || !g || world == 0 || rank >= world) return set_error(KCLPP_ERR_INVALID, "kclpp_graph_shard: bad argument");
+  KCL_TRY(set_device(c));
+  g->owner.assign(g->dag.n, 0);
+  if (world > 1) shard_plan_host(g->dag.n, g->dag.off.data(), world, g->owner.data());
+  g->shard_rank = rank;
+  g->shard_world = world;
+  cudaFree(g->d_roots);
+  g->d_roots = nullptr;
+  KCL_TRY(build_schedule(c, g));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_seq_delta_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, const uint64_t *r_dev, uint64_t *delta_dev) {
+  if (!c || !gc || ((!r_dev || !delta_dev) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  if (!g->dag.n) return KCLPP_OK;
+  KCL_CUDA(cudaMemsetAsync(delta_dev, 0, (size_t)g->dag.n * 8, c->stream));
+  dev::PassArgs a{};
+  a.r_in = (const unsigned long long *)r_dev;
+  a.out = (unsigned long long *)delta_dev;
+  return run_tiers(c, g, dev::MODE_SEQ, k, a);
+}
+
+kclpp_status kclpp_sim_counts_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, const double *rho_dev, uint64_t *cnt_dev) {
+  if (!c || !gc || ((!rho_dev || !cnt_dev) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 2));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  if (!g->dag.n) return KCLPP_OK;
+  return sim_counts_dev(c, g, k, rho_dev, (unsigned long long *)cnt_dev);
+}
+
+kclpp_status kclpp_sim_update_dev(kclpp_ctx *c, uint32_t n, uint32_t t, double *rho_dev, const uint64_t *cnt_dev) {
+  if (!c || ((!rho_dev || !cnt_dev) && n) || t < 1) return set_error(KCLPP_ERR_INVALID, "bad argument");
+  KCL_TRY(set_device(c));
+  if (!n) return KCLPP_OK;
+  k_sim_update<<<blocks_for(n), 256, 0, c->stream>>>(rho_dev, (const unsigned long long *)cnt_dev, n, t);
+  KCL_CUDA(cudaGetLastError());
+  c->launches++;
+  return KCLPP_OK;
 }
 
 // ---- sort, PAVA, densest prefix ------------------------------------------------------

@@ -106,11 +106,19 @@ struct TierLaunch {
 cudaError_t launch_count(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st);
 cudaError_t launch_order(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st);
 cudaError_t launch_seq(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st);
-// Threads per CTA for a tier.
+// Threads per CTA for a tier.  Tier M / L CTAs of the Seq kernel are wider:
+// their warps each run one root-edge stream, and 12 of them fit twice per SM
+// at out-degree 610 (the counting kernels' warps share one bitmap per CTA).
 constexpr int kWarpsS = 4;
 constexpr int kWarpsM = 8;
-// Tier bounds on a root's out-degree.
+constexpr int kWarpsMSeq = 12;
+template <int MODE>
+constexpr int warps_m() { return MODE == dev::MODE_SEQ ? kWarpsMSeq : kWarpsM; }
+// Tier bounds on a root's out-degree.  The Seq kernel keeps only the smallest
+// roots on tier S (a lane runs a whole root-edge stream there, which is slow
+// on dense roots); the counting kernels use tier S up to 64.
 constexpr uint32_t kTierSMax = 64;
+constexpr uint32_t kTierSMaxSeq = 16;
 constexpr uint32_t kTierMMax = 1024;
 constexpr uint32_t kTierLMax = 2048;
 

@@ -61,11 +61,12 @@ static cudaError_t noalloc_tier(int tier, dev::PassArgs a, int sms, cudaStream_t
     return cudaGetLastError();
   }
   static LaunchCache lc;
-  const size_t sm = layout_m(MODE_COUNT, a.dmax, kWarpsM, true).total;
+  constexpr int NW = warps_m<MODE_COUNT>();
+  const size_t sm = layout_m(MODE_COUNT, a.dmax, NW, true).total;
   auto fn = tier_m_kernel<MODE_COUNT, K, 1, true, true>;
-  cudaError_t e = prepare(fn, lc, kWarpsM * 32, sm, &per_sm);
+  cudaError_t e = prepare(fn, lc, NW * 32, sm, &per_sm);
   if (e != cudaSuccess) return e;
-  fn<<<per_sm * sms, kWarpsM * 32, sm, st>>>(a);
+  fn<<<per_sm * sms, NW * 32, sm, st>>>(a);
   return cudaGetLastError();
 }
 

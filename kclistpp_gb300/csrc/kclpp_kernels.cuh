@@ -403,62 +403,50 @@ __host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, boo
 }
 
 // The Seq chain over V (last level) from prefix argmin g, 32 candidates at a time.
+//
+// Compaction: the candidates are written to the warp's buffer in ascending
+// order one nonzero word at a time, a lane per bit (position = candidates
+// before the word + set bits of the word below the lane), so no lane loops
+// over its own bits.  Each chunk of 32 then resolves the chain by the ballot
+// fixed point on 32-bit distances: rel = cur[v] - c (clamped; -1 when cur[v]
+// is below c, which always succeeds), and candidate i fails iff rel_i >= the
+// failures before it in the chunk.
 template <int WPL>
 __device__ __forceinline__ uint32_t chain_warp(const Bits<WPL> &V, int g, const unsigned long long *base,
                                                uint32_t *dl, uint16_t *buf, int lane, uint32_t *err) {
-  int cntl = popc_lane(V);
-  int incl = cntl;
+  const uint32_t lt = lanemask_lt();
+  uint32_t total = 0;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(KCL_FULL, incl, o);
-    if (lane >= o) incl += t;
+  for (int q = 0; q < WPL; ++q) {
+    uint32_t nz = __ballot_sync(KCL_FULL, V.w[q] != 0);
+    while (nz) {
+      const int L = __ffs(nz) - 1;
+      nz &= nz - 1;
+      const uint32_t word = __shfl_sync(KCL_FULL, V.w[q], L);
+      if ((word >> lane) & 1u) buf[total + __popc(word & lt)] = (uint16_t)(((L + 32 * q) << 5) | lane);
+      total += (uint32_t)__popc(word);
+    }
   }
-  const int total = __shfl_sync(KCL_FULL, incl, 31);
   if (total == 0) return 0;
-  // Ascending order across lanes: lane-major per word group q.  With WPL > 1
-  // the words of lane l are l and l + 32, so order the groups first.
-  if (WPL == 1) {
-    int pos = incl - cntl;
-    uint32_t w = V.w[0];
-    while (w) {
-      const int b = __ffs(w) - 1;
-      w &= w - 1;
-      buf[pos++] = (uint16_t)(lane * 32 + b);
-    }
-  } else {
-    int before = 0;
-#pragma unroll
-    for (int q = 0; q < WPL; ++q) {
-      const int cq = __popc(V.w[q]);
-      int iq = cq;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(KCL_FULL, iq, o);
-        if (lane >= o) iq += t;
-      }
-      int pos = before + iq - cq;
-      uint32_t w = V.w[q];
-      while (w) {
-        const int b = __ffs(w) - 1;
-        w &= w - 1;
-        buf[pos++] = (uint16_t)((lane + 32 * q) * 32 + b);
-      }
-      before += __shfl_sync(KCL_FULL, iq, 31);
-    }
-  }
   __syncwarp();
   const unsigned long long c0 = base[g] + dl[g];
   unsigned long long c = c0;
-  const uint32_t lt = lanemask_lt();
-  for (int b0 = 0; b0 < total; b0 += 32) {
-    const int idx = b0 + lane;
+  for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+    const uint32_t idx = b0 + lane;
     const bool valid = idx < total;
     const int v = valid ? buf[idx] : 0;
-    const unsigned long long av = valid ? base[v] + dl[v] : 0ull;
-    uint32_t m = __ballot_sync(KCL_FULL, valid && av >= c);
+    int rel = -1;
+    if (valid) {
+      const unsigned long long av = base[v] + dl[v];
+      if (av >= c) {
+        const unsigned long long dd = av - c;
+        rel = dd > 0x7fffffffull ? 0x7fffffff : (int)dd;
+      }
+    }
+    uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
     for (int r = 0; r < 33; ++r) {
-      const uint32_t f = (uint32_t)__popc(m & lt);
-      const uint32_t m2 = __ballot_sync(KCL_FULL, valid && av >= c + f);
+      const int f = __popc(m & lt);
+      const uint32_t m2 = __ballot_sync(KCL_FULL, rel >= f);
       if (m2 == m) break;
       m = m2;
     }
@@ -475,7 +463,7 @@ __device__ __forceinline__ uint32_t chain_warp(const Bits<WPL> &V, int g, const 
     dl[g] = (uint32_t)nd;
   }
   __syncwarp();
-  return (uint32_t)total;
+  return total;
 }
 
 template <int L, int WPL>
@@ -527,9 +515,9 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
 }
 
 template <int MODE, int K, int WPL, bool ROWS_IN_SMEM, bool IDENT = false>
-__global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
+__global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int NW = kWarpsM;
+  constexpr int NW = warps_m<MODE>();
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int dmax = (int)a.dmax;
   const LayoutM lay = layout_m(MODE, a.dmax, NW, ROWS_IN_SMEM);
@@ -561,7 +549,7 @@ __global__ void __launch_bounds__(kWarpsM * 32) tier_m_kernel(PassArgs a) {
         idx = atomicAdd(a.work, 1u);
         if (idx >= a.num_roots) stealing = true;
       }
-      if (stealing) idx = find_victim<IDENT>(a, K - 1);
+      if (stealing) idx = a.steal_cursor ? find_victim<IDENT>(a, K - 1) : UINT32_MAX;
       s_idx = idx;
       s_tau = 0;
       s_sum = 0;
@@ -796,21 +784,22 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
     fn<<<persistent_grid(per_sm, t, kWarpsS, false), kWarpsS * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
+  constexpr int NW = warps_m<MODE>();
   if (t.tier == 1) {
     static LaunchCache lc;
-    const size_t sm = layout_m(MODE, t.dmax, kWarpsM, true).total;
+    const size_t sm = layout_m(MODE, t.dmax, NW, true).total;
     auto fn = tier_m_kernel<MODE, K, 1, true>;
-    cudaError_t e = prepare(fn, lc, kWarpsM * 32, sm, &per_sm);
+    cudaError_t e = prepare(fn, lc, NW * 32, sm, &per_sm);
     if (e != cudaSuccess) return e;
-    fn<<<persistent_grid(per_sm, t, 1, true), kWarpsM * 32, sm, st>>>(a);
+    fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), NW * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
   static LaunchCache lc;
-  const size_t sm = layout_m(MODE, t.dmax, kWarpsM, false).total;
+  const size_t sm = layout_m(MODE, t.dmax, NW, false).total;
   auto fn = tier_m_kernel<MODE, K, 2, false>;
-  cudaError_t e = prepare(fn, lc, kWarpsM * 32, sm, &per_sm);
+  cudaError_t e = prepare(fn, lc, NW * 32, sm, &per_sm);
   if (e != cudaSuccess) return e;
-  fn<<<persistent_grid(per_sm, t, 1, true), kWarpsM * 32, sm, st>>>(a);
+  fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), NW * 32, sm, st>>>(a);
   return cudaGetLastError();
 }
 
