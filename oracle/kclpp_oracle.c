@@ -414,8 +414,8 @@ static uint64_t visit_rec(orc_ws *w, visit_t *vt, int l, uint32_t best, int dept
 /* Shared driver for order-free passes (CDF_CliqueEnum, kCDensestNoAtom.c:270-313
  * and kCDensestCmpSync.c:298-325): dynamic schedule over root edges, per-thread
  * counters merged at the end (integers, so the merge order is immaterial).  */
-static uint64_t visit_all(const orc_graph *g, int k, visit_t proto, uint64_t nout,
-                          uint64_t *out, int threads, uint64_t stride) {
+static uint64_t visit_all_masked(const orc_graph *g, int k, visit_t proto, uint64_t nout,
+                                 uint64_t *out, int threads, uint64_t stride, const uint8_t *root_mask) {
   uint64_t total = 0;
   if (stride == 0) stride = 1;
   memset(out, 0, (size_t)nout * sizeof(uint64_t));
@@ -430,6 +430,7 @@ static uint64_t visit_all(const orc_graph *g, int k, visit_t proto, uint64_t nou
     for (int64_t q = 0; q < ne; ++q) {
       uint64_t i = (uint64_t)q * stride;
       uint32_t s = g->edges[i].s, t = g->edges[i].t;
+      if (root_mask && !root_mask[s]) continue;
       uint32_t b;
       if (vt.kind == 2) {
         b = 0;
@@ -453,6 +454,11 @@ static uint64_t visit_all(const orc_graph *g, int k, visit_t proto, uint64_t nou
   return total;
 }
 
+static uint64_t visit_all(const orc_graph *g, int k, visit_t proto, uint64_t nout,
+                          uint64_t *out, int threads, uint64_t stride) {
+  return visit_all_masked(g, k, proto, nout, out, threads, stride, NULL);
+}
+
 uint64_t orc_count_cliques(const orc_graph *g, int k, uint64_t *per_vertex) {
   visit_t p;
   memset(&p, 0, sizeof p);
@@ -464,8 +470,8 @@ uint64_t orc_count_cliques(const orc_graph *g, int k, uint64_t *per_vertex) {
 }
 
 /* ---- Seq-kClist++ pass, CDF_CliqueEnum FRANK_WOLFE, kCDensestNoAtom.c:270-295. */
-static uint64_t seq_pass_impl(const orc_graph *g, int k, uint64_t *rho, int mode, int threads,
-                              uint64_t stride) {
+static uint64_t seq_pass_impl_masked(const orc_graph *g, int k, uint64_t *rho, int mode, int threads,
+                                     uint64_t stride, const uint8_t *root_mask) {
   const uint32_t n = g->n;
   uint64_t total = 0;
   if (stride == 0) stride = 1;
@@ -500,6 +506,7 @@ static uint64_t seq_pass_impl(const orc_graph *g, int k, uint64_t *rho, int mode
     for (int64_t q = 0; q < ne; ++q) {
       uint64_t i = (uint64_t)q * stride;
       uint32_t s = g->edges[i].s, t = g->edges[i].t;
+      if (root_mask && !root_mask[s]) continue;
       uint32_t ngw = cur[t] < cur[s] ? t : s;
       make_subgraph(w, g, s, t);
       total += seq_rec(w, cur, k - 2, ngw);
@@ -530,6 +537,34 @@ static uint64_t seq_pass_impl(const orc_graph *g, int k, uint64_t *rho, int mode
   free(delta);
   free(rho_old);
   return total;
+}
+
+static uint64_t seq_pass_impl(const orc_graph *g, int k, uint64_t *rho, int mode, int threads,
+                              uint64_t stride) {
+  return seq_pass_impl_masked(g, k, rho, mode, threads, stride, NULL);
+}
+
+/* Per-root-edge-stream increments of the root edges whose source is marked
+ * in root_mask (one shard of a split pass): delta = r_after - r. */
+int orc_seq_delta_masked(const orc_graph *g, int k, const uint64_t *rho, const uint8_t *root_mask, int threads,
+                         uint64_t *delta) {
+  if (k < 3 || k >= ORC_MAXK) return -1;
+  uint64_t *tmp = (uint64_t *)xmalloc(((size_t)g->n + 1) * sizeof(uint64_t));
+  memcpy(tmp, rho, (size_t)g->n * sizeof(uint64_t));
+  seq_pass_impl_masked(g, k, tmp, ORC_SEQ_EDGE_STREAMS, threads, 1, root_mask);
+  for (uint32_t x = 0; x < g->n; ++x) delta[x] = tmp[x] - rho[x];
+  free(tmp);
+  return 0;
+}
+
+/* Sim rho_add of the marked roots' cliques. */
+void orc_sim_counts_masked(const orc_graph *g, int k, const double *rho, const uint8_t *root_mask, int threads,
+                           uint64_t *cnt) {
+  visit_t p;
+  memset(&p, 0, sizeof p);
+  p.kind = 0;
+  p.rho = rho;
+  visit_all_masked(g, k, p, g->n, cnt, threads, 1, root_mask);
 }
 
 int orc_seq_pass(const orc_graph *g, int k, uint64_t *rho, int mode, int threads) {

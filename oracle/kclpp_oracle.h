@@ -71,10 +71,16 @@ void orc_sort_by_r_u64(uint32_t n, const uint64_t *rho, uint32_t *reordered);
 /* Sampled pass for the timed CPU baseline: every stride-th root edge; returns cliques visited. */
 uint64_t orc_seq_pass_sample(const orc_graph *g, int k, uint64_t *rho, int mode, int threads, uint64_t stride);
 
+/* One shard of a split pass: only root edges whose source is marked. */
+int orc_seq_delta_masked(const orc_graph *g, int k, const uint64_t *rho, const uint8_t *root_mask, int threads,
+                         uint64_t *delta);
+
 /* ---- Sim-kClist++ (kCDensestCmpSync.c) --------------------------------- */
 void orc_sim_counts(const orc_graph *g, int k, const double *rho, uint64_t *cnt, int threads);
 uint64_t orc_sim_counts_sample(const orc_graph *g, int k, const double *rho, uint64_t *cnt, int threads,
                                uint64_t stride);
+void orc_sim_counts_masked(const orc_graph *g, int k, const double *rho, const uint8_t *root_mask, int threads,
+                           uint64_t *cnt);
 void orc_sim_update(uint32_t n, uint32_t t, double *rho, const uint64_t *cnt);
 void orc_sim_pava(const orc_graph *g, int k, const uint32_t *level, uint64_t *tentative, int threads);
 orc_info orc_sim_find_densest(const orc_graph *g, int k, const double *rho,

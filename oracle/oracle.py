@@ -86,6 +86,8 @@ def lib() -> C.CDLL:
             "orc_free_trim": (None, [C.POINTER(OrcTrim)]),
             "orc_seq_main": (C.c_int, [G, C.c_int, C.c_uint32, C.c_int, C.c_int, u64p, C.POINTER(OrcInfo), C.c_int]),
             "orc_sim_main": (C.c_int, [G, C.c_int, C.c_uint32, C.c_int, f64p, C.POINTER(OrcInfo), C.c_int]),
+            "orc_seq_delta_masked": (C.c_int, [G, C.c_int, u64p, C.POINTER(C.c_uint8), C.c_int, u64p]),
+            "orc_sim_counts_masked": (None, [G, C.c_int, f64p, C.POINTER(C.c_uint8), C.c_int, u64p]),
             "orc_wtime": (C.c_double, []),
             "orc_max_threads": (C.c_int, []),
         }
@@ -192,6 +194,22 @@ class Graph:
         tent = np.zeros(self.n + 1, dtype=np.uint64)
         lib().orc_seq_pava(self._g, k, _p(level, C.c_uint32), _p(tent, C.c_uint64), threads)
         return tent[: self.n]
+
+    def seq_delta_masked(self, k: int, r: np.ndarray, mask: np.ndarray, threads: int = 1) -> np.ndarray:
+        """Increments of one shard's root edges (EDGE_STREAMS order)."""
+        r = np.ascontiguousarray(r, dtype=np.uint64)
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        d = np.zeros(self.n + 1, dtype=np.uint64)
+        if lib().orc_seq_delta_masked(self._g, k, _p(r, C.c_uint64), _p(m, C.c_uint8), threads, _p(d, C.c_uint64)):
+            raise ValueError("oracle: unsupported k")
+        return d[: self.n]
+
+    def sim_counts_masked(self, k: int, rho: np.ndarray, mask: np.ndarray, threads: int = 1) -> np.ndarray:
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        m = np.ascontiguousarray(mask, dtype=np.uint8)
+        cnt = np.zeros(self.n + 1, dtype=np.uint64)
+        lib().orc_sim_counts_masked(self._g, k, _p(rho, C.c_double), _p(m, C.c_uint8), threads, _p(cnt, C.c_uint64))
+        return cnt[: self.n]
 
     def count_edges(self, nodes: np.ndarray) -> int:
         nodes = np.ascontiguousarray(nodes, dtype=np.uint32)
