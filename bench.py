@@ -224,6 +224,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "kclpp_bench_cache"))
     a = ap.parse_args()
     modes = [m for m in a.modes.split(",") if m]
@@ -285,9 +286,18 @@ def main() -> None:
     el = K.EdgeList.from_pairs(pairs)
     g = K.build_graph(ctx, el)
     off, cols = g.csr()
+    tuned = {}
+    if not a.no_autotune:
+        # Untimed setup: pick the fastest schedule for each kernel of the step.
+        for md, kern in (("seq", K.KERNEL_SEQ), ("sim", K.KERNEL_ORDER)):
+            if md in modes:
+                t = K.autotune(g, a.k, kern)
+                tuned[md] = {"schedule": t.best.as_dict(), "pass_ms": t.best_ms, "default_pass_ms": t.default_ms,
+                             "candidates": t.candidates}
     cliques_per_pass, _ = K.count_cliques(g, a.k)
     stats = dag_stats(off, cols, a.k, 64)
     stats_seq = dag_stats(off, cols, a.k, 16)
+    config["autotune"] = tuned
     config["dag"] = {"n": g.n, "m": g.m, "max_out_degree": g.core, "cliques_per_pass": int(cliques_per_pass),
                      "tiers": {f"{t}{d}": v for (t, d), v in stats["tiers"].items()},
                      "seq_tiers": {f"{t}{d}": v for (t, d), v in stats_seq["tiers"].items()}}

@@ -130,6 +130,54 @@ void kclpp_graph_free(kclpp_graph *g);
 kclpp_status kclpp_count_edges(kclpp_ctx *ctx, const kclpp_graph *g, uint32_t num_nodes,
                                const uint32_t *nodes, uint32_t *m_out);
 
+/* Schedule knobs of a device graph (no reference counterpart).  Roots are
+ * split into tiers by out-degree: tier S (a warp per root, out-degree <= 64),
+ * tier M (a CTA per root, rows in shared memory, out-degree <= 1024, launched
+ * in three groups bounded by m_split1 and m_split2 so that smaller roots get a
+ * smaller shared-memory footprint and more CTAs per SM), tier L (beyond).
+ * Work stealing lets CTAs without a root of their own join unfinished roots. */
+typedef struct {
+  uint32_t tier_s_max;      /* counting kernels (k-clique degrees, Sim, PAVA): tier S bound, <= 64 */
+  uint32_t tier_s_max_seq;  /* Seq kernel: tier S bound, <= 64                                    */
+  uint32_t m_split1, m_split2; /* tier M groups: (S, split1], (split1, split2], (split2, 1024]    */
+  int steal_seq;            /* work stealing in the Seq kernel                                    */
+  int steal_count;          /* work stealing in the counting kernels                              */
+} kclpp_schedule;
+kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp);
+kclpp_status kclpp_graph_set_schedule(kclpp_ctx *ctx, kclpp_graph *g, const kclpp_schedule *sp);
+/* Autotuner: times one pass of `kernel` (KCLPP_KERNEL_SEQ or KCLPP_KERNEL_ORDER)
+ * at clique size k under each candidate schedule, keeps the fastest on g and
+ * reports it.  r / rho start from zero; results are unaffected by the choice. */
+typedef struct {
+  kclpp_schedule best;
+  double best_ms;           /* one pass under the chosen schedule   */
+  double default_ms;        /* one pass under the default schedule  */
+  int candidates;
+} kclpp_tune_result;
+kclpp_status kclpp_autotune(kclpp_ctx *ctx, kclpp_graph *g, int k, int kernel, kclpp_tune_result *out);
+
+/* ---- batches (no reference counterpart) ----------------------------------
+ * Many graphs of uneven size as one disjoint union on the device (each graph
+ * keeps its own degeneracy order), run for several k values at once: every
+ * pass of every k is recorded into one CUDA graph (one concurrent branch per
+ * k, each pass one launch per tier over all graphs' roots) that is launched
+ * with a single call.  Results equal separate runs of each graph. */
+typedef struct kclpp_batch kclpp_batch;
+kclpp_status kclpp_batch_create(kclpp_ctx *ctx, const kclpp_edge_list *const *els, uint32_t count,
+                                kclpp_batch **out);
+/* union_graph (borrowed, may be NULL) can be tuned with kclpp_autotune. */
+kclpp_status kclpp_batch_info(const kclpp_batch *b, uint32_t *graphs, uint32_t *total_n, uint64_t *total_m,
+                              kclpp_graph **union_graph);
+/* offsets[i] = first union vertex of graph i (graphs + 1 entries). */
+kclpp_status kclpp_batch_vertex_offsets(const kclpp_batch *b, uint32_t *offsets);
+/* `passes` Seq (KCLPP_KERNEL_SEQ, r u64) or Sim (KCLPP_KERNEL_ORDER, rho f64)
+ * passes from zero for each of ks[0..nk); out (host) receives nk vectors of
+ * total_n entries, k-major.  The captured graph is reused while kernel, ks
+ * and passes stay the same. */
+kclpp_status kclpp_batch_run(kclpp_ctx *ctx, kclpp_batch *b, int kernel, const int *ks, int nk,
+                             uint32_t passes, void *out);
+void kclpp_batch_free(kclpp_batch *b);
+
 /* ---- k-clique counts (A16 on the DAG) ----------------------------------- */
 /* Number of k-cliques and, if per_vertex != NULL, the k-clique degree of every
  * vertex (onepass/recursion, kClistCoreTrim.c:368-416). */

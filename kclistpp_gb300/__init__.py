@@ -73,6 +73,21 @@ KERNEL_NAMES = {0: "count", 1: "order", 2: "seq"}
 TIER_NAMES = {0: "S", 1: "M", 2: "L"}
 
 
+class Schedule(C.Structure):
+    _fields_ = [("tier_s_max", C.c_uint32), ("tier_s_max_seq", C.c_uint32), ("m_split1", C.c_uint32),
+                ("m_split2", C.c_uint32), ("steal_seq", C.c_int), ("steal_count", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("best", Schedule), ("best_ms", C.c_double), ("default_ms", C.c_double), ("candidates", C.c_int)]
+
+
+KERNEL_COUNT, KERNEL_ORDER, KERNEL_SEQ = 0, 1, 2
+
+
 class GenParams(C.Structure):
     _fields_ = [("kind", C.c_int), ("n", C.c_uint32), ("avg_degree", C.c_double),
                 ("gamma", C.c_double), ("scale", C.c_uint32), ("edge_factor", C.c_uint32),
@@ -120,6 +135,14 @@ _SIGS = {
     "kclpp_graph_free": (None, [_P]),
     "kclpp_count_edges": (C.c_int, [_P, _P, C.c_uint32, _u32p, _u32p]),
     "kclpp_count_cliques": (C.c_int, [_P, _P, C.c_int, _u64p, _u64p]),
+    "kclpp_graph_get_schedule": (C.c_int, [_P, C.POINTER(Schedule)]),
+    "kclpp_graph_set_schedule": (C.c_int, [_P, _P, C.POINTER(Schedule)]),
+    "kclpp_autotune": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
+    "kclpp_batch_create": (C.c_int, [_P, C.POINTER(_P), C.c_uint32, C.POINTER(_P)]),
+    "kclpp_batch_info": (C.c_int, [_P, _u32p, _u32p, _u64p, C.POINTER(_P)]),
+    "kclpp_batch_vertex_offsets": (C.c_int, [_P, _u32p]),
+    "kclpp_batch_run": (C.c_int, [_P, _P, C.c_int, C.POINTER(C.c_int), C.c_int, C.c_uint32, _P]),
+    "kclpp_batch_free": (None, [_P]),
     "kclpp_count_cliques_noalloc": (C.c_int, [_P, C.c_uint32, C.c_uint64, _P, _P, C.c_int, _P, _u64p]),
     "kclpp_seq_passes": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _u64p]),
     "kclpp_seq_passes_dev": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_int, _P]),
@@ -318,9 +341,9 @@ class Graph:
         return off, cols
 
     def close(self):
-        if getattr(self, "_h", None):
+        if getattr(self, "_h", None) and not getattr(self, "_borrowed", False):
             _lib.kclpp_graph_free(self._h)
-            self._h = None
+        self._h = None
 
     def __del__(self):
         self.close()
@@ -343,6 +366,67 @@ def graph_from_csr(ctx: Context, offsets: np.ndarray, cols: np.ndarray) -> Graph
     _check(_lib.kclpp_graph_from_csr(ctx.handle, len(off) - 1, len(cl), _ptr(off, C.c_uint64),
                                      _ptr(cl, C.c_uint32), C.byref(h)))
     return Graph(ctx, h)
+
+
+def get_schedule(g: Graph) -> Schedule:
+    sp = Schedule()
+    _check(_lib.kclpp_graph_get_schedule(g._h, C.byref(sp)))
+    return sp
+
+
+def set_schedule(g: Graph, sp: Schedule) -> None:
+    _check(_lib.kclpp_graph_set_schedule(g.ctx.handle, g._h, C.byref(sp)))
+
+
+def autotune(g: Graph, k: int, kernel: int = KERNEL_SEQ) -> TuneResult:
+    """Time one pass under each candidate schedule and keep the fastest on g."""
+    r = TuneResult()
+    _check(_lib.kclpp_autotune(g.ctx.handle, g._h, k, kernel, C.byref(r)))
+    return r
+
+
+class Batch:
+    """Many graphs as one device union, run for several k values in one captured CUDA graph."""
+
+    def __init__(self, ctx: Context, edge_lists: list[EdgeList]):
+        self.ctx = ctx
+        arr = (_P * max(1, len(edge_lists)))(*[e._h for e in edge_lists])
+        h = _P()
+        _check(_lib.kclpp_batch_create(ctx.handle, arr, len(edge_lists), C.byref(h)))
+        self._h = h
+        gs, n, m, ug = C.c_uint32(), C.c_uint32(), C.c_uint64(), _P()
+        _check(_lib.kclpp_batch_info(h, C.byref(gs), C.byref(n), C.byref(m), C.byref(ug)))
+        self.graphs, self.n, self.m = gs.value, n.value, m.value
+        self._union = ug
+        self.offsets = np.empty(self.graphs + 1, dtype=np.uint32)
+        _check(_lib.kclpp_batch_vertex_offsets(h, _ptr(self.offsets, C.c_uint32)))
+
+    def union_graph(self) -> "Graph":
+        """The union DAG (borrowed; valid while the batch lives)."""
+        g = Graph.__new__(Graph)
+        g.ctx, g._h, g.n, g.m, g.core = self.ctx, self._union, self.n, self.m, 0
+        g._borrowed = True
+        return g
+
+    def run(self, kernel: int, ks: list[int], passes: int) -> np.ndarray:
+        """(len(ks), n) array: Seq r (uint64) or Sim rho (float64) after `passes` passes."""
+        dt = np.uint64 if kernel == KERNEL_SEQ else np.float64
+        out = np.empty((len(ks), self.n), dtype=dt)
+        kk = (C.c_int * len(ks))(*ks)
+        _check(_lib.kclpp_batch_run(self.ctx.handle, self._h, kernel, kk, len(ks), passes,
+                                    out.ctypes.data_as(_P)))
+        return out
+
+    def slice(self, i: int) -> slice:
+        return slice(int(self.offsets[i]), int(self.offsets[i + 1]))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.kclpp_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
 
 
 def count_edges(g: Graph, nodes: np.ndarray) -> int:

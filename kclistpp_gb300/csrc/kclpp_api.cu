@@ -73,6 +73,8 @@ struct TierInfo {
 struct kclpp_graph {
   int device = 0;
   HostDag dag;
+  // Schedule knobs (tier bounds, stealing); the autotuner may change them.
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0};
   uint64_t *d_off = nullptr;
   uint32_t *d_cols = nullptr;
   uint32_t *d_src = nullptr;
@@ -92,6 +94,7 @@ struct kclpp_graph {
   uint32_t *d_work = nullptr;   // [0,16): root counters per tier; [16,32): steal cursors
   uint32_t *d_task = nullptr;   // per-root sub-task counters (tiers M, L)
   uint32_t num_roots = 0;
+  uint32_t task_cap = 0;
   unsigned long long *d_scalar = nullptr;
   uint32_t *d_slab = nullptr;
   uint64_t slab_words = 0;
@@ -192,7 +195,7 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
   bool any_l = false;
   uint32_t mx = 0;
   for (int sch = 0; sch < 2; ++sch) {
-    const uint32_t smax = sch == 0 ? kTierSMax : kTierSMaxSeq;
+    const uint32_t smax = sch == 0 ? g->sp.tier_s_max : g->sp.tier_s_max_seq;
     std::vector<uint32_t> tS, tM1, tM2, tM3, tL;
     for (uint32_t s = 0; s < D.n; ++s) {
       const uint32_t d = deg(s);
@@ -200,8 +203,8 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
       if (g->shard_world > 1 && g->owner[s] != g->shard_rank) continue;
       mx = std::max(mx, d);
       if (d <= smax) tS.push_back(s);
-      else if (d <= 256) tM1.push_back(s);
-      else if (d <= 512) tM2.push_back(s);
+      else if (d <= g->sp.m_split1) tM1.push_back(s);
+      else if (d <= g->sp.m_split2) tM2.push_back(s);
       else if (d <= kTierMMax) tM3.push_back(s);
       else tL.push_back(s);
     }
@@ -231,7 +234,13 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
   if (!all.empty())
     KCL_CUDA(cudaMemcpyAsync(g->d_roots, all.data(), all.size() * 4, cudaMemcpyHostToDevice, c->stream));
   KCL_TRY(dalloc(&g->d_work, 32));
+  if (g->num_roots > g->task_cap) {  // the counters must cover every root of the schedule
+    cudaFree(g->d_task);
+    g->d_task = nullptr;
+    g->task_cap = 0;
+  }
   KCL_TRY(dalloc(&g->d_task, g->num_roots));
+  g->task_cap = std::max(g->task_cap, std::max<uint32_t>(g->num_roots, 1));
   if (any_l) {
     g->slab_ctas = c->num_sms;
     const uint64_t W = (kTierLMax + 31) / 32;
@@ -274,13 +283,23 @@ static void free_graph_dev(kclpp_graph *g) {
   cudaFree(g->d_work); cudaFree(g->d_task); cudaFree(g->d_scalar); cudaFree(g->d_slab);
 }
 
+// Where a pass runs: its stream and its scheduler counters.  Concurrent passes
+// (the batch's k values) each need their own counters.
+struct Exec {
+  cudaStream_t st;
+  uint32_t *work;  // 32 words
+  uint32_t *task;  // one per root
+};
+
 // Launch every tier of one mode.
-static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev::PassArgs a) {
+static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev::PassArgs a,
+                              const Exec *ex = nullptr) {
   const int sch = mode == dev::MODE_SEQ ? 1 : 0;
   const std::vector<TierInfo> &tiers = g->tiers[sch];
   if (tiers.empty()) return KCLPP_OK;
-  KCL_CUDA(cudaMemsetAsync(g->d_work, 0, 32 * sizeof(uint32_t), c->stream));
-  KCL_CUDA(cudaMemsetAsync(g->d_task, 0, (size_t)g->num_roots * sizeof(uint32_t), c->stream));
+  const Exec E = ex ? *ex : Exec{c->stream, g->d_work, g->d_task};
+  KCL_CUDA(cudaMemsetAsync(E.work, 0, 32 * sizeof(uint32_t), E.st));
+  KCL_CUDA(cudaMemsetAsync(E.task, 0, (size_t)g->num_roots * sizeof(uint32_t), E.st));
   a.off = g->d_off;
   a.cols = g->d_cols;
   a.err = c->d_err;
@@ -293,25 +312,27 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     tl.roots = g->d_roots + t.offset;
     tl.num_roots = t.count;
     tl.dmax = t.dmax;
-    tl.work = g->d_work + i;
-    tl.task_next = g->d_task + (t.offset - g->sched_base[sch]);
+    tl.work = E.work + i;
+    tl.task_next = E.task + (t.offset - g->sched_base[sch]);
     // Work stealing pays off for the Seq chains (long, uneven root edges); the
-    // counting kernels finish their roots quickly and do not steal.
-    tl.steal_cursor = mode == dev::MODE_SEQ ? g->d_work + 16 + i : nullptr;
+    // counting kernels finish their roots quickly and by default do not steal.
+    const bool steal = mode == dev::MODE_SEQ ? g->sp.steal_seq != 0 : g->sp.steal_count != 0;
+    tl.steal_cursor = steal ? E.work + 16 + i : nullptr;
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
     cudaError_t e = cudaSuccess;
     PendingTime pt{mode, t.tier, t.dmax, nullptr, nullptr};
-    if (c->profile) {
+    const bool prof = c->profile && !ex;
+    if (prof) {
       pt.a = take_event(c);
       pt.b = take_event(c);
-      if (pt.a) cudaEventRecord(pt.a, c->stream);
+      if (pt.a) cudaEventRecord(pt.a, E.st);
     }
-    if (mode == dev::MODE_COUNT) e = launch_count(k, tl, a, c->stream);
-    else if (mode == dev::MODE_ORDER) e = launch_order(k, tl, a, c->stream);
-    else e = launch_seq(k, tl, a, c->stream);
-    if (c->profile && pt.a && pt.b) {
-      cudaEventRecord(pt.b, c->stream);
+    if (mode == dev::MODE_COUNT) e = launch_count(k, tl, a, E.st);
+    else if (mode == dev::MODE_ORDER) e = launch_order(k, tl, a, E.st);
+    else e = launch_seq(k, tl, a, E.st);
+    if (prof && pt.a && pt.b) {
+      cudaEventRecord(pt.b, E.st);
       c->pending.push_back(pt);
     }
     if (e != cudaSuccess)
@@ -737,6 +758,312 @@ kclpp_status kclpp_sim_update_dev(kclpp_ctx *c, uint32_t n, uint32_t t, double *
   KCL_CUDA(cudaGetLastError());
   c->launches++;
   return KCLPP_OK;
+}
+
+// ---- schedule knobs and the autotuner ----------------------------------------------------
+static kclpp_status check_schedule(const kclpp_schedule *sp) {
+  if (sp->tier_s_max > kTierSMax || sp->tier_s_max_seq > kTierSMax || sp->m_split1 < sp->tier_s_max ||
+      sp->m_split1 < sp->tier_s_max_seq || sp->m_split2 < sp->m_split1 || sp->m_split2 > kTierMMax)
+    return set_error(KCLPP_ERR_INVALID, "schedule bounds out of range (tier S <= %u <= split1 <= split2 <= %u)",
+                     kTierSMax, kTierMMax);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp) {
+  if (!g || !sp) return set_error(KCLPP_ERR_INVALID, "null argument");
+  *sp = g->sp;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_graph_set_schedule(kclpp_ctx *c, kclpp_graph *g, const kclpp_schedule *sp) {
+  if (!c || !g || !sp) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_schedule(sp));
+  KCL_TRY(set_device(c));
+  g->sp = *sp;
+  cudaFree(g->d_roots);
+  g->d_roots = nullptr;
+  KCL_TRY(build_schedule(c, g));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  return KCLPP_OK;
+}
+
+// One pass of `mode` from a zero vector, timed with events on the context's stream.
+static kclpp_status time_pass(kclpp_ctx *c, kclpp_graph *g, int k, int mode, float *ms) {
+  const size_t bytes = (size_t)g->dag.n * 8;
+  cudaEvent_t e0 = take_event(c), e1 = take_event(c);
+  if (!e0 || !e1) return set_error(KCLPP_ERR_CUDA, "event creation failed");
+  for (int rep = 0; rep < 2; ++rep) {  // the first run warms caches and loads the kernel
+    if (mode == dev::MODE_SEQ) {
+      KCL_CUDA(cudaMemsetAsync(g->d_a, 0, bytes, c->stream));
+      KCL_CUDA(cudaEventRecord(e0, c->stream));
+      KCL_TRY(seq_pass_dev(c, g, k, g->d_a, g->d_b, nullptr));
+    } else {
+      KCL_CUDA(cudaMemsetAsync(g->d_rho, 0, bytes, c->stream));
+      KCL_CUDA(cudaEventRecord(e0, c->stream));
+      KCL_TRY(sim_counts_dev(c, g, k, g->d_rho, g->d_a));
+    }
+    KCL_CUDA(cudaEventRecord(e1, c->stream));
+  }
+  KCL_CUDA(cudaEventSynchronize(e1));
+  KCL_CUDA(cudaEventElapsedTime(ms, e0, e1));
+  c->event_pool.push_back(e0);
+  c->event_pool.push_back(e1);
+  return check_err(c);
+}
+
+kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kclpp_tune_result *out) {
+  if (!c || !g || !out) return set_error(KCLPP_ERR_INVALID, "null argument");
+  if (kernel != KCLPP_KERNEL_SEQ && kernel != KCLPP_KERNEL_ORDER)
+    return set_error(KCLPP_ERR_INVALID, "autotune: kernel must be KCLPP_KERNEL_SEQ or KCLPP_KERNEL_ORDER");
+  KCL_TRY(check_k(k, kernel == KCLPP_KERNEL_SEQ ? 3 : 2));
+  KCL_TRY(set_device(c));
+  memset(out, 0, sizeof *out);
+  const int mode = kernel == KCLPP_KERNEL_SEQ ? dev::MODE_SEQ : dev::MODE_ORDER;
+  const kclpp_schedule base = g->sp;
+  std::vector<kclpp_schedule> cand;
+  const uint32_t smax[3] = {8, 16, 32};
+  const uint32_t smax_count[2] = {32, 64};
+  const uint32_t splits[2][2] = {{256, 512}, {384, 768}};
+  for (int sp = 0; sp < 2; ++sp)
+    for (int st = 0; st < 2; ++st) {
+      if (mode == dev::MODE_SEQ) {
+        for (uint32_t sm : smax) {
+          kclpp_schedule x = base;
+          x.tier_s_max_seq = sm;
+          x.m_split1 = splits[sp][0];
+          x.m_split2 = splits[sp][1];
+          x.steal_seq = st == 0;
+          cand.push_back(x);
+        }
+      } else {
+        for (uint32_t sm : smax_count) {
+          kclpp_schedule x = base;
+          x.tier_s_max = sm;
+          x.m_split1 = splits[sp][0];
+          x.m_split2 = splits[sp][1];
+          x.steal_count = st;
+          cand.push_back(x);
+        }
+      }
+    }
+  float best = 1e30f, def = 0.f;
+  kclpp_schedule best_sp = base;
+  {
+    float ms = 0.f;
+    KCL_TRY(time_pass(c, g, k, mode, &ms));
+    def = ms;
+    best = ms;
+  }
+  for (const kclpp_schedule &x : cand) {
+    KCL_TRY(kclpp_graph_set_schedule(c, g, &x));
+    float ms = 0.f;
+    KCL_TRY(time_pass(c, g, k, mode, &ms));
+    if (ms < best) { best = ms; best_sp = x; }
+  }
+  KCL_TRY(kclpp_graph_set_schedule(c, g, &best_sp));
+  out->best = best_sp;
+  out->best_ms = best;
+  out->default_ms = def;
+  out->candidates = (int)cand.size() + 1;
+  return KCLPP_OK;
+}
+
+// ---- batches: many graphs and several k values in one captured CUDA graph -----------------
+}  // extern "C"
+
+struct BatchBranch {
+  int k = 0;
+  cudaStream_t st = nullptr;
+  cudaEvent_t join = nullptr;
+  uint32_t *work = nullptr, *task = nullptr;
+  unsigned long long *buf[2] = {nullptr, nullptr};  // Seq ping-pong, or Sim counts in buf[0]
+  double *rho = nullptr;
+  void *result = nullptr;  // device vector holding the branch's final r / rho
+};
+
+struct kclpp_batch {
+  kclpp_graph *g = nullptr;
+  std::vector<uint32_t> voff;  // per graph: first vertex in the union
+  std::vector<BatchBranch> br;
+  cudaEvent_t fork = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int exec_kernel = -1;
+  std::vector<int> exec_ks;
+  uint32_t exec_passes = 0;
+};
+
+static void batch_release(kclpp_batch *b) {
+  for (auto &x : b->br) {
+    if (x.st) cudaStreamDestroy(x.st);
+    if (x.join) cudaEventDestroy(x.join);
+    cudaFree(x.work); cudaFree(x.task); cudaFree(x.buf[0]); cudaFree(x.buf[1]); cudaFree(x.rho);
+  }
+  b->br.clear();
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+}
+
+extern "C" {
+
+kclpp_status kclpp_batch_create(kclpp_ctx *c, const kclpp_edge_list *const *els, uint32_t count, kclpp_batch **out) {
+  if (!c || !out || (!els && count)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  *out = nullptr;
+  KCL_TRY(set_device(c));
+  auto *g = new kclpp_graph();
+  std::vector<uint32_t> voff(1, 0);
+  uint64_t m = 0;
+  std::vector<HostDag> dags(count);
+  for (uint32_t i = 0; i < count; ++i) {
+    if (!els[i]) { delete g; return set_error(KCLPP_ERR_INVALID, "batch: null edge list %u", i); }
+    std::vector<uint32_t> rank(els[i]->n);
+    core_order_host(els[i]->n, els[i]->pairs, rank.data());
+    kclpp_status s = make_dag_host(els[i]->pairs, rank.data(), dags[i]);
+    if (s != KCLPP_OK) { delete g; return s; }
+    if ((uint64_t)voff.back() + dags[i].n > UINT32_MAX) { delete g; return set_error(KCLPP_ERR_UNSUPPORTED, "batch: more than 2^32 vertices"); }
+    voff.push_back(voff.back() + dags[i].n);
+    m += dags[i].m();
+  }
+  // Disjoint union: graph i's vertices are shifted by voff[i]; every row stays
+  // ascending and below its source, so the union is a DAG of the same kind.
+  HostDag &U = g->dag;
+  U.n = voff.back();
+  U.off.assign((size_t)U.n + 1, 0);
+  U.cols.resize(m);
+  uint64_t at = 0;
+  uint32_t core = 0;
+  for (uint32_t i = 0; i < count; ++i) {
+    const HostDag &D = dags[i];
+    for (uint32_t s = 0; s < D.n; ++s) {
+      U.off[voff[i] + s] = at;
+      for (uint64_t e = D.off[s]; e < D.off[s + 1]; ++e) U.cols[at++] = D.cols[e] + voff[i];
+    }
+    core = std::max(core, D.core);
+  }
+  U.off[U.n] = at;
+  U.core = core;
+  kclpp_graph *gg = nullptr;
+  KCL_TRY(finish_graph(c, g, &gg));
+  auto *b = new kclpp_batch();
+  b->g = gg;
+  b->voff = std::move(voff);
+  *out = b;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_batch_info(const kclpp_batch *b, uint32_t *graphs, uint32_t *total_n, uint64_t *total_m,
+                              kclpp_graph **union_graph) {
+  if (!b) return set_error(KCLPP_ERR_INVALID, "null batch");
+  if (graphs) *graphs = (uint32_t)b->voff.size() - 1;
+  if (total_n) *total_n = b->g->dag.n;
+  if (total_m) *total_m = b->g->dag.m();
+  if (union_graph) *union_graph = b->g;
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_batch_vertex_offsets(const kclpp_batch *b, uint32_t *offsets) {
+  if (!b || !offsets) return set_error(KCLPP_ERR_INVALID, "null argument");
+  memcpy(offsets, b->voff.data(), b->voff.size() * 4);
+  return KCLPP_OK;
+}
+
+// Record every branch's passes on its own stream (inside or outside a capture).
+static kclpp_status batch_record(kclpp_ctx *c, kclpp_batch *b, int kernel, uint32_t passes) {
+  kclpp_graph *g = b->g;
+  const uint32_t n = g->dag.n;
+  KCL_CUDA(cudaEventRecord(b->fork, c->stream));
+  for (auto &x : b->br) {
+    KCL_CUDA(cudaStreamWaitEvent(x.st, b->fork, 0));
+    const Exec E{x.st, x.work, x.task};
+    if (kernel == KCLPP_KERNEL_SEQ) {
+      KCL_CUDA(cudaMemsetAsync(x.buf[0], 0, (size_t)n * 8, x.st));
+      int cur = 0;
+      for (uint32_t p = 0; p < passes; ++p) {
+        KCL_CUDA(cudaMemcpyAsync(x.buf[cur ^ 1], x.buf[cur], (size_t)n * 8, cudaMemcpyDeviceToDevice, x.st));
+        dev::PassArgs a{};
+        a.r_in = x.buf[cur];
+        a.out = x.buf[cur ^ 1];
+        KCL_TRY(run_tiers(c, g, dev::MODE_SEQ, x.k, a, &E));
+        cur ^= 1;
+      }
+      x.result = x.buf[cur];
+    } else {
+      KCL_CUDA(cudaMemsetAsync(x.rho, 0, (size_t)n * 8, x.st));
+      for (uint32_t p = 0; p < passes; ++p) {
+        KCL_CUDA(cudaMemsetAsync(x.buf[0], 0, (size_t)n * 8, x.st));
+        dev::PassArgs a{};
+        a.key_kind = dev::KEY_SIM;
+        a.rho = x.rho;
+        a.out = x.buf[0];
+        KCL_TRY(run_tiers(c, g, dev::MODE_ORDER, x.k, a, &E));
+        k_sim_update<<<blocks_for(n), 256, 0, x.st>>>(x.rho, x.buf[0], n, p + 1);
+        KCL_CUDA(cudaGetLastError());
+        c->launches++;
+      }
+      x.result = x.rho;
+    }
+    KCL_CUDA(cudaEventRecord(x.join, x.st));
+    KCL_CUDA(cudaStreamWaitEvent(c->stream, x.join, 0));
+  }
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_batch_run(kclpp_ctx *c, kclpp_batch *b, int kernel, const int *ks, int nk, uint32_t passes,
+                             void *out) {
+  if (!c || !b || !ks || nk <= 0 || (!out && b->g->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  if (kernel != KCLPP_KERNEL_SEQ && kernel != KCLPP_KERNEL_ORDER)
+    return set_error(KCLPP_ERR_INVALID, "batch: kernel must be KCLPP_KERNEL_SEQ or KCLPP_KERNEL_ORDER (Sim)");
+  for (int i = 0; i < nk; ++i) KCL_TRY(check_k(ks[i], kernel == KCLPP_KERNEL_SEQ ? 3 : 2));
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = b->g;
+  const uint32_t n = g->dag.n;
+  if (!n) return KCLPP_OK;
+  const std::vector<int> want(ks, ks + nk);
+  const bool same = b->exec && b->exec_kernel == kernel && b->exec_ks == want && b->exec_passes == passes;
+  if (!same) {
+    batch_release(b);
+    if (!b->fork) KCL_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->br.resize(nk);
+    for (int i = 0; i < nk; ++i) {
+      BatchBranch &x = b->br[i];
+      x.k = ks[i];
+      KCL_CUDA(cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking));
+      KCL_CUDA(cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming));
+      KCL_TRY(dalloc(&x.work, 32));
+      KCL_TRY(dalloc(&x.task, std::max<uint32_t>(g->num_roots, 1)));
+      KCL_TRY(dalloc(&x.buf[0], n));
+      if (kernel == KCLPP_KERNEL_SEQ) KCL_TRY(dalloc(&x.buf[1], n));
+      else KCL_TRY(dalloc(&x.rho, n));
+    }
+    // One run outside the capture settles the kernels' launch settings.
+    KCL_TRY(batch_record(c, b, kernel, std::min<uint32_t>(passes, 1)));
+    KCL_CUDA(cudaStreamSynchronize(c->stream));
+    cudaGraph_t graph = nullptr;
+    KCL_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+    kclpp_status rs = batch_record(c, b, kernel, passes);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (rs != KCLPP_OK) { if (graph) cudaGraphDestroy(graph); return rs; }
+    if (ce != cudaSuccess) return set_error(KCLPP_ERR_CUDA, "batch capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return set_error(KCLPP_ERR_CUDA, "batch instantiate: %s", cudaGetErrorString(ce));
+    b->exec_kernel = kernel;
+    b->exec_ks = want;
+    b->exec_passes = passes;
+  }
+  KCL_CUDA(cudaGraphLaunch(b->exec, c->stream));
+  c->launches++;
+  for (int i = 0; i < nk; ++i)
+    KCL_CUDA(cudaMemcpyAsync((char *)out + (size_t)i * n * 8, b->br[i].result, (size_t)n * 8,
+                             cudaMemcpyDeviceToHost, c->stream));
+  return check_err(c);
+}
+
+void kclpp_batch_free(kclpp_batch *b) {
+  if (!b) return;
+  batch_release(b);
+  if (b->fork) cudaEventDestroy(b->fork);
+  kclpp_graph_free(b->g);
+  delete b;
 }
 
 // ---- sort, PAVA, densest prefix ------------------------------------------------------
