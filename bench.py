@@ -405,26 +405,44 @@ def main() -> None:
         cols_h[:] = cols
         r_h = torch.zeros(n, dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
         rho_h = torch.zeros(n, dtype=torch.float64, pin_memory=True).numpy()
-        K.seq_passes_csr(ctx, off_h, cols_h, a.k, 1, r_h)  # warm
+        import ctypes as C
+
+        sched = {md: K.Schedule(**tuned[md]["schedule"]) for md in tuned}
+
+        def e2e_step(tt):
+            # The public host-buffer path: upload the DAG, choose the schedule,
+            # run one pass of each kernel on host r / rho, download them.
+            g2 = K.graph_from_csr(ctx, off_h, cols_h)
+            for md in modes:
+                if md in sched:
+                    K.set_schedule(g2, sched[md])
+                if md == "seq":
+                    K._check(K._lib.kclpp_seq_passes(ctx.handle, g2._h, a.k, 1, K.SEQ_EDGE_STREAMS,
+                                                     r_h.ctypes.data_as(C.POINTER(C.c_uint64))))
+                else:
+                    K._check(K._lib.kclpp_sim_passes(ctx.handle, g2._h, a.k, tt, 1,
+                                                     rho_h.ctypes.data_as(C.POINTER(C.c_double))))
+            g2.close()
+
+        e2e_step(1)  # warm
         e2e_t = []
-        tt = 1
+        tt = 2
         for _ in range(a.e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            for md in modes:
-                if md == "seq":
-                    K.seq_passes_csr(ctx, off_h, cols_h, a.k, 1, r_h)
-                else:
-                    K.sim_passes_csr(ctx, off_h, cols_h, a.k, 1, rho_h, t_first=tt)
-                    tt += 1
+            e2e_step(tt)
+            tt += 1
             e2e_t.append(time.perf_counter() - t0)
         roots = int(np.count_nonzero(np.diff(off)))
-        graph_bytes = 8 * (n + 1) + 4 * g.m + 4 * g.m + 4 * roots
-        h2d = len(modes) * (graph_bytes + 8 * n)
-        d2h = len(modes) * (8 * n + 4)
+        # offsets, columns, edge sources, both root schedules (again per
+        # schedule change), and r / rho
+        graph_bytes = 8 * (n + 1) + 4 * g.m + 4 * g.m + 8 * roots * (1 + len(sched))
+        h2d = graph_bytes + 8 * n * len(modes)
+        d2h = (8 * n + 4) * len(modes)
         e2e = {"value": per_step / statistics.median(e2e_t), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": a.e2e_steps,
-               "api": "kclpp_seq_passes_csr / kclpp_sim_passes_csr (host CSR + host r, pinned)"}
+               "api": "kclpp_graph_from_csr + kclpp_graph_set_schedule + kclpp_seq_passes / kclpp_sim_passes "
+                      "(host CSR + host r / rho, pinned)"}
 
     cpu = None
     if rank == 0 and world == 1 and not a.no_cpu:

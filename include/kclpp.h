@@ -295,6 +295,45 @@ kclpp_status kclpp_sim_main(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_
                             double *rho_out, kclpp_densest_info *infos, int max_infos,
                             int *n_infos);
 
+/* ---- learned warm start (no reference counterpart) ------------------------------
+ * A 4 -> 64 (ReLU) -> 1 MLP, bf16 weights with fp32 accumulation, predicts
+ * each vertex's Seq-kClist++ load log1p(r / T) from the features
+ * log1p([degree, core number, triangles, 4-cliques capped at 2^24]).  The
+ * forward, backward and Adam kernels are the library's own.  A warm start
+ * begins the passes at r0 = round(t0 * predicted load); its upper bound must
+ * come from the increments r - r0 (kclpp_extract_densest_seq_warm), which
+ * remain a feasible load, while the plain zero-start run stays the fallback. */
+typedef struct kclpp_warm_model kclpp_warm_model;
+#define KCLPP_WARM_FEATURES 4
+#define KCLPP_WARM_HIDDEN 64
+#define KCLPP_WARM_PARAMS (KCLPP_WARM_HIDDEN * KCLPP_WARM_FEATURES + 2 * KCLPP_WARM_HIDDEN + 1)
+kclpp_status kclpp_warm_create(kclpp_ctx *ctx, uint64_t seed, kclpp_warm_model **out);
+void kclpp_warm_free(kclpp_warm_model *m);
+/* fp32 master parameters, KCLPP_WARM_PARAMS floats: W1 (64 x 4, row-major), b1, W2, b2. */
+kclpp_status kclpp_warm_get_params(const kclpp_warm_model *m, float *params);
+kclpp_status kclpp_warm_set_params(kclpp_ctx *ctx, kclpp_warm_model *m, const float *params);
+/* Features of every vertex of g into X_dev (n x 4 floats, device). */
+kclpp_status kclpp_warm_features(kclpp_ctx *ctx, const kclpp_graph *g, float *X_dev);
+kclpp_status kclpp_warm_features_dev(kclpp_ctx *ctx, uint32_t n, const uint32_t *deg_dev, const uint32_t *core_dev,
+                                     const uint64_t *tri_dev, const uint64_t *k4_dev, float *X_dev);
+/* Y_dev[i] = model(X_dev[i]) (device, enqueued). */
+kclpp_status kclpp_warm_predict_dev(kclpp_ctx *ctx, const kclpp_warm_model *m, const float *X_dev, uint32_t n,
+                                    float *Y_dev);
+/* Gradient of the mean squared error over the n rows (host outputs, either may be NULL). */
+kclpp_status kclpp_warm_grad_dev(kclpp_ctx *ctx, kclpp_warm_model *m, const float *X_dev, const float *Y_dev,
+                                 uint32_t n, float *grad_host, float *loss_host);
+/* `steps` full-batch Adam steps (learning rate lr); loss_host gets the final loss. */
+kclpp_status kclpp_warm_train(kclpp_ctx *ctx, kclpp_warm_model *m, const float *X_dev, const float *Y_dev,
+                              uint32_t n, uint32_t steps, float lr, float *loss_host);
+kclpp_status kclpp_warm_r0_dev(kclpp_ctx *ctx, const float *Y_dev, uint32_t n, float t0, uint64_t *r0_dev);
+/* features + prediction + r0 for g in one call (r0_dev: n entries, device). */
+kclpp_status kclpp_warm_start_r(kclpp_ctx *ctx, const kclpp_graph *g, const kclpp_warm_model *m, float t0,
+                                uint64_t *r0_dev);
+/* Densest prefix in the order of r (host) with the upper bound of the T
+ * passes' increments r - r0 (host), for runs that started at r0. */
+kclpp_status kclpp_extract_densest_seq_warm(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t T,
+                                            const uint64_t *r, const uint64_t *r0, kclpp_densest_info *info);
+
 /* ---- k-clique core trim (A15-A18) ------------------------------------------ */
 #define KCLPP_TRIM_EXACT 0  /* the reference's heap peel: core numbers, peel order,
                                best suffix and trimmed set identical to it */

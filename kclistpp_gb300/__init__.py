@@ -167,6 +167,18 @@ _SIGS = {
                                  C.c_int, C.POINTER(C.c_int)]),
     "kclpp_sim_main": (C.c_int, [_P, _P, C.c_int, C.c_uint32, _f64p, C.POINTER(DensestInfo), C.c_int,
                                  C.POINTER(C.c_int)]),
+    "kclpp_warm_create": (C.c_int, [_P, C.c_uint64, C.POINTER(_P)]),
+    "kclpp_warm_free": (None, [_P]),
+    "kclpp_warm_get_params": (C.c_int, [_P, C.POINTER(C.c_float)]),
+    "kclpp_warm_set_params": (C.c_int, [_P, _P, C.POINTER(C.c_float)]),
+    "kclpp_warm_features": (C.c_int, [_P, _P, _P]),
+    "kclpp_warm_features_dev": (C.c_int, [_P, C.c_uint32, _P, _P, _P, _P, _P]),
+    "kclpp_warm_predict_dev": (C.c_int, [_P, _P, _P, C.c_uint32, _P]),
+    "kclpp_warm_grad_dev": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "kclpp_warm_train": (C.c_int, [_P, _P, _P, _P, C.c_uint32, C.c_uint32, C.c_float, C.POINTER(C.c_float)]),
+    "kclpp_warm_r0_dev": (C.c_int, [_P, _P, C.c_uint32, C.c_float, _P]),
+    "kclpp_warm_start_r": (C.c_int, [_P, _P, _P, C.c_float, _P]),
+    "kclpp_extract_densest_seq_warm": (C.c_int, [_P, _P, C.c_int, C.c_uint32, _u64p, _u64p, C.POINTER(DensestInfo)]),
     "kclpp_trim": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(_P)]),
     "kclpp_trim_info_get": (C.c_int, [_P, C.POINTER(TrimInfo)]),
     "kclpp_trim_copy": (C.c_int, [_P, _u32p, _u64p, _u32p, _u64p]),
@@ -542,6 +554,16 @@ def extract_densest_seq(g: Graph, k: int, T: int, r: np.ndarray) -> tuple[Denses
     _check(_lib.kclpp_extract_densest_seq(g.ctx.handle, g._h, k, T, _ptr(r, C.c_uint64), C.byref(info),
                                           _ptr(re, C.c_uint32)))
     return info, re
+
+
+def extract_densest_seq_warm(g: Graph, k: int, T: int, r: np.ndarray, r0: np.ndarray) -> DensestInfo:
+    """Densest prefix in the order of r; upper bound from the increments r - r0 of T passes."""
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    r0 = np.ascontiguousarray(r0, dtype=np.uint64)
+    info = DensestInfo()
+    _check(_lib.kclpp_extract_densest_seq_warm(g.ctx.handle, g._h, k, T, _ptr(r, C.c_uint64), _ptr(r0, C.c_uint64),
+                                               C.byref(info)))
+    return info
 
 
 def extract_densest_sim(g: Graph, k: int, rho: np.ndarray) -> tuple[DensestInfo, np.ndarray]:

@@ -1304,3 +1304,156 @@ kclpp_status kclpp_sim_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t
 }
 
 }  // extern "C"
+
+// ---- context accessors for the other translation units ------------------------------------
+namespace kclpp {
+cudaStream_t ctx_stream(kclpp_ctx *c) { return c->stream; }
+int ctx_device(kclpp_ctx *c) { return c->device; }
+int ctx_sms(kclpp_ctx *c) { return c->num_sms; }
+void ctx_count_launch(kclpp_ctx *c, int n) { c->launches += (uint64_t)n; }
+}  // namespace kclpp
+
+// ---- learned warm start: graph-level pieces -------------------------------------------------
+// Core numbers of the undirected graph behind a DAG (bucket peel, O(n + m)).
+static void core_numbers_host(const HostDag &D, std::vector<uint32_t> &deg, std::vector<uint32_t> &core) {
+  const uint32_t n = D.n;
+  deg.assign(n, 0);
+  for (uint32_t s = 0; s < n; ++s) {
+    deg[s] += (uint32_t)(D.off[s + 1] - D.off[s]);
+    for (uint64_t e = D.off[s]; e < D.off[s + 1]; ++e) deg[D.cols[e]]++;
+  }
+  std::vector<uint64_t> cu((size_t)n + 1, 0);
+  for (uint32_t v = 0; v < n; ++v) cu[v + 1] = cu[v] + deg[v];
+  std::vector<uint32_t> adj(cu[n]);
+  {
+    std::vector<uint64_t> f(cu.begin(), cu.end() - 1);
+    for (uint32_t s = 0; s < n; ++s)
+      for (uint64_t e = D.off[s]; e < D.off[s + 1]; ++e) {
+        adj[f[s]++] = D.cols[e];
+        adj[f[D.cols[e]]++] = s;
+      }
+  }
+  uint32_t md = 0;
+  for (uint32_t v = 0; v < n; ++v) md = std::max(md, deg[v]);
+  std::vector<uint32_t> cur(deg), bin((size_t)md + 2, 0), pos(n), vert(n);
+  for (uint32_t v = 0; v < n; ++v) bin[cur[v]]++;
+  uint32_t start = 0;
+  for (uint32_t d = 0; d <= md; ++d) { uint32_t c = bin[d]; bin[d] = start; start += c; }
+  for (uint32_t v = 0; v < n; ++v) { pos[v] = bin[cur[v]]; vert[pos[v]] = v; bin[cur[v]]++; }
+  for (uint32_t d = md + 1; d >= 1; --d) bin[d] = bin[d - 1];
+  bin[0] = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t v = vert[i];
+    for (uint64_t e = cu[v]; e < cu[v + 1]; ++e) {
+      const uint32_t u = adj[e];
+      if (cur[u] > cur[v]) {
+        const uint32_t du = cur[u], pu = pos[u], pw = bin[du], w = vert[pw];
+        if (u != w) { pos[u] = pw; vert[pu] = w; pos[w] = pu; vert[pw] = u; }
+        bin[du]++;
+        cur[u]--;
+      }
+    }
+  }
+  core.swap(cur);
+}
+
+extern "C" {
+
+kclpp_status kclpp_warm_features(kclpp_ctx *c, const kclpp_graph *gc, float *X_dev) {
+  if (!c || !gc || (!X_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  const uint32_t n = g->dag.n;
+  if (!n) return KCLPP_OK;
+  std::vector<uint32_t> deg, core;
+  core_numbers_host(g->dag, deg, core);
+  uint32_t *d_deg = nullptr, *d_core = nullptr;
+  KCL_CUDA(cudaMalloc((void **)&d_deg, (size_t)n * 4));
+  std::unique_ptr<uint32_t, decltype(&cudaFree)> g1(d_deg, &cudaFree);
+  KCL_CUDA(cudaMalloc((void **)&d_core, (size_t)n * 4));
+  std::unique_ptr<uint32_t, decltype(&cudaFree)> g2(d_core, &cudaFree);
+  KCL_CUDA(cudaMemcpyAsync(d_deg, deg.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  KCL_CUDA(cudaMemcpyAsync(d_core, core.data(), (size_t)n * 4, cudaMemcpyHostToDevice, c->stream));
+  // triangles and 4-cliques per vertex with the count kernels
+  for (int k = 3; k <= 4; ++k) {
+    unsigned long long *out = k == 3 ? g->d_a : g->d_b;
+    KCL_CUDA(cudaMemsetAsync(out, 0, (size_t)n * 8, c->stream));
+    dev::PassArgs a{};
+    a.out = out;
+    KCL_TRY(run_tiers(c, g, dev::MODE_COUNT, k, a));
+  }
+  KCL_TRY(kclpp_warm_features_dev(c, n, d_deg, d_core, (const uint64_t *)g->d_a, (const uint64_t *)g->d_b, X_dev));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  return check_err(c);
+}
+
+kclpp_status kclpp_warm_start_r(kclpp_ctx *c, const kclpp_graph *gc, const kclpp_warm_model *M, float t0,
+                                uint64_t *r0_dev) {
+  if (!c || !gc || !M || (!r0_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(set_device(c));
+  const uint32_t n = gc->dag.n;
+  if (!n) return KCLPP_OK;
+  float *X = nullptr, *Y = nullptr;
+  KCL_CUDA(cudaMalloc((void **)&X, (size_t)n * 16));
+  std::unique_ptr<float, decltype(&cudaFree)> g1(X, &cudaFree);
+  KCL_CUDA(cudaMalloc((void **)&Y, (size_t)n * 4));
+  std::unique_ptr<float, decltype(&cudaFree)> g2(Y, &cudaFree);
+  KCL_TRY(kclpp_warm_features(c, gc, X));
+  KCL_TRY(kclpp_warm_predict_dev(c, M, X, n, Y));
+  KCL_TRY(kclpp_warm_r0_dev(c, Y, n, t0, r0_dev));
+  KCL_CUDA(cudaStreamSynchronize(c->stream));
+  return check_err(c);
+}
+
+kclpp_status kclpp_extract_densest_seq_warm(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t T,
+                                            const uint64_t *r, const uint64_t *r0, kclpp_densest_info *info) {
+  if (!c || !gc || !info || ((!r || !r0) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_k(k, 3));
+  if (T < 1) return set_error(KCLPP_ERR_INVALID, "T must be >= 1");
+  KCL_TRY(set_device(c));
+  kclpp_graph *g = const_cast<kclpp_graph *>(gc);
+  memset(info, 0, sizeof *info);
+  const uint32_t n = g->dag.n;
+  if (!n) return KCLPP_OK;
+  // Densest prefix in the order of r (warm start included): the same scan as
+  // kCDensestNoAtom.c:341-349 on exact prefix clique counts.
+  std::vector<uint32_t> reordered(n), level(n);
+  KCL_TRY(kclpp_sort_by_r_u64(c, n, r, reordered.data(), level.data()));
+  std::vector<uint64_t> tent;
+  KCL_TRY(pava_and_edges(c, g, k, level, tent));
+  double density = -1;
+  unsigned long long sum = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += tent[i];
+    if ((double)sum / (i + 1) > density) {
+      density = (double)sum / (i + 1);
+      info->n = i + 1;
+      info->cliques = sum;
+    }
+  }
+  info->density = density;
+  KCL_TRY(edges_in_prefix(c, g, info->n, &info->m));
+  // Upper bound from the loads the T passes added: (r - r0) / T is a feasible
+  // fractional assignment of the cliques (every pass gives each clique one
+  // unit), and the bound of kCDensestNoAtom.c:352-369 needs the loads in
+  // descending order of the loads themselves.
+  std::vector<uint64_t> inc(n);
+  for (uint32_t i = 0; i < n; ++i) inc[i] = r[i] - r0[i];
+  std::sort(inc.begin(), inc.end(), std::greater<uint64_t>());
+  sum = 0;
+  double ub = 0, ip1ck = 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += inc[i];
+    if (i + 1 == (uint32_t)k) ip1ck = 1;
+    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
+    if (ip1ck < (double)sum / T) ub = ip1ck / (i + 1);
+    else {
+      if (ub < (double)sum / T / (i + 1)) ub = (double)sum / T / (i + 1);
+      break;
+    }
+  }
+  info->ub = ub;
+  return KCLPP_OK;
+}
+
+}  // extern "C"

@@ -7,6 +7,8 @@
 
 #include "../../include/kclpp.h"
 
+typedef struct CUstream_st *cudaStream_t;
+
 struct kclpp_edge_list {
   uint32_t n = 0;               // max id + 1 (ReadEdgeList semantics)
   std::vector<uint32_t> pairs;  // s0 t0 s1 t1 ...
@@ -43,6 +45,12 @@ struct HostDag {
   std::vector<uint32_t> cols;     // m, ascending per row, cols < row
   uint64_t m() const { return cols.size(); }
 };
+
+// Context accessors for translation units other than the one defining kclpp_ctx.
+cudaStream_t ctx_stream(kclpp_ctx *c);
+int ctx_device(kclpp_ctx *c);
+int ctx_sms(kclpp_ctx *c);
+void ctx_count_launch(kclpp_ctx *c, int n);
 
 // SortByCore with the reference heap's tie order.
 void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank);
