@@ -33,11 +33,17 @@ def _torch():
     return torch
 
 
+# The library runs on its context's stream and torch on its own: every hand-over
+# of a tensor between the two waits for the producer.
+def _after_torch():
+    _torch().cuda.synchronize()
+
+
 def features(g: Graph):
     """(n, 4) float32 device tensor of the model's inputs for g."""
     torch = _torch()
     X = torch.empty((g.n, 4), dtype=torch.float32, device="cuda")
-    _check(_lib.kclpp_warm_features(g.ctx.handle, g._h, C.c_void_p(X.data_ptr())))
+    _check(_lib.kclpp_warm_features(g.ctx.handle, g._h, C.c_void_p(X.data_ptr())))  # synchronises
     return X
 
 
@@ -74,6 +80,7 @@ class WarmModel:
 
     def predict(self, X):
         torch = _torch()
+        _after_torch()
         Y = torch.empty(X.shape[0], dtype=torch.float32, device="cuda")
         _check(_lib.kclpp_warm_predict_dev(self.ctx.handle, self._h, C.c_void_p(X.data_ptr()), X.shape[0],
                                            C.c_void_p(Y.data_ptr())))
@@ -81,6 +88,7 @@ class WarmModel:
         return Y
 
     def grad(self, X, Y) -> tuple[np.ndarray, float]:
+        _after_torch()
         g = np.empty(NPARAMS, dtype=np.float32)
         loss = C.c_float()
         _check(_lib.kclpp_warm_grad_dev(self.ctx.handle, self._h, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()),
@@ -88,6 +96,7 @@ class WarmModel:
         return g, loss.value
 
     def train(self, X, Y, steps: int = 400, lr: float = 1e-2) -> float:
+        _after_torch()
         loss = C.c_float()
         _check(_lib.kclpp_warm_train(self.ctx.handle, self._h, C.c_void_p(X.data_ptr()), C.c_void_p(Y.data_ptr()),
                                      X.shape[0], steps, lr, C.byref(loss)))
@@ -120,6 +129,7 @@ def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, mode
     t_start = time.perf_counter()
     if model is None:
         r_dev = torch.zeros(g.n, dtype=torch.int64, device="cuda")
+        _after_torch()
         r0 = None
     else:
         r_dev = model.start_r(g, t0)
@@ -129,6 +139,7 @@ def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, mode
     p = 0
     while p < max_passes:
         seq_passes_dev(g, k, 1, r_dev.data_ptr())
+        g.ctx.synchronize()
         p += 1
         r = r_dev.cpu().numpy().view(np.uint64)
         info = extract_densest_seq(g, k, p, r)[0] if r0 is None else extract_densest_seq_warm(g, k, p, r, r0)

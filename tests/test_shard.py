@@ -99,18 +99,22 @@ def test_split_pass_on_gpu(ctx):
         acc_r = torch.zeros(n, dtype=torch.int64, device="cuda")
         acc_c = torch.zeros(n, dtype=torch.int64, device="cuda")
         part = torch.empty(n, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()  # the library runs on its own stream
         for rank in range(WORLD):
             K.graph_shard(g, rank, WORLD)
             K.seq_delta_dev(g, k, r_d.data_ptr(), part.data_ptr())
             ctx.synchronize()
             acc_r += part
+            torch.cuda.synchronize()
             K.sim_counts_dev(g, k, rho_d.data_ptr(), part.data_ptr())
             ctx.synchronize()
             acc_c += part
+            torch.cuda.synchronize()
         K.graph_shard(g, 0, 1)
         assert np.array_equal(r0 + acc_r.cpu().numpy().view(np.uint64), full_r)
         assert np.array_equal(acc_c.cpu().numpy().view(np.uint64), full_c)
         # the Sim update on the summed counts equals the unsplit pass
+        torch.cuda.synchronize()
         K.sim_update_dev(ctx, n, 1, rho_d.data_ptr(), acc_c.data_ptr())
         ctx.synchronize()
         assert np.array_equal(rho_d.cpu().numpy().view(np.uint64), K.sim_passes(g, k, 1, rho0).view(np.uint64))
