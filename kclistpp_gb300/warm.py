@@ -119,11 +119,12 @@ class WarmModel:
 
 
 def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, model: WarmModel | None = None,
-                t0: float = 16.0) -> dict:
+                t0: float = 16.0, trace: bool = False) -> dict:
     """Run Seq passes (per-root-edge streams) until (ub - density) / ub <= gap.
 
     Zero start when model is None; otherwise start at r0 = model.start_r(g, t0)
-    (the features, the inference and r0 are inside the timed region)."""
+    (the features, the inference and r0 are inside the timed region).  With
+    trace=True the result also holds every pass's (seconds, density, ub)."""
     torch = _torch()
     torch.cuda.synchronize()
     t_start = time.perf_counter()
@@ -137,15 +138,29 @@ def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, mode
     info = DensestInfo()
     reached = False
     p = 0
+    hist = []
     while p < max_passes:
         seq_passes_dev(g, k, 1, r_dev.data_ptr())
         g.ctx.synchronize()
         p += 1
         r = r_dev.cpu().numpy().view(np.uint64)
         info = extract_densest_seq(g, k, p, r)[0] if r0 is None else extract_densest_seq_warm(g, k, p, r, r0)
+        if trace:
+            hist.append((time.perf_counter() - t_start, info.density, info.ub))
         if info.ub > 0 and (info.ub - info.density) / info.ub <= gap:
             reached = True
             break
     torch.cuda.synchronize()
-    return {"passes": p, "seconds": time.perf_counter() - t_start, "reached": reached,
-            "density": info.density, "ub": info.ub, "n": info.n, "cliques": info.cliques}
+    out = {"passes": p, "seconds": time.perf_counter() - t_start, "reached": reached,
+           "density": info.density, "ub": info.ub, "n": info.n, "cliques": info.cliques}
+    if trace:
+        out["trace"] = hist
+    return out
+
+
+def passes_to_density(trace: list, target: float) -> tuple[int, float]:
+    """First pass (and its elapsed seconds) whose prefix density reaches target."""
+    for i, (sec, dens, _) in enumerate(trace):
+        if dens >= target:
+            return i + 1, sec
+    return len(trace) + 1, float("inf")
