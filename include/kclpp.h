@@ -93,6 +93,7 @@ void kclpp_edge_list_free(kclpp_edge_list *el);
 #define KCLPP_GEN_RMAT 2
 #define KCLPP_GEN_ER 3
 #define KCLPP_GEN_PLANTED 4     /* Chung-Lu base plus planted G(n_c, p) communities */
+#define KCLPP_GEN_RMAT_PLANTED 5 /* RMAT base plus planted G(n_c, p) communities   */
 typedef struct {
   int kind;
   uint32_t n;                   /* vertices (CHUNG_LU, ER, PLANTED)             */
@@ -101,7 +102,7 @@ typedef struct {
   uint32_t scale;               /* RMAT: n = 2^scale                            */
   uint32_t edge_factor;         /* RMAT: samples = edge_factor * n              */
   double a, b, c;               /* RMAT quadrant probabilities (d = 1-a-b-c)    */
-  uint32_t communities;         /* PLANTED                                      */
+  uint32_t communities;         /* PLANTED, RMAT_PLANTED                        */
   uint32_t comm_min, comm_max;  /* PLANTED: sizes log-uniform in [min, max]     */
   double p_in;                  /* PLANTED: edge probability inside             */
   uint64_t seed;
@@ -142,6 +143,7 @@ typedef struct {
   uint32_t m_split1, m_split2; /* tier M groups: (S, split1], (split1, split2], (split2, 1024]    */
   int steal_seq;            /* work stealing in the Seq kernel                                    */
   int steal_count;          /* work stealing in the counting kernels                              */
+  uint32_t seq_waves;       /* waves of KCLPP_SEQ_WAVES, 1..1024 (default 16)                     */
 } kclpp_schedule;
 kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp);
 kclpp_status kclpp_graph_set_schedule(kclpp_ctx *ctx, kclpp_graph *g, const kclpp_schedule *sp);
@@ -207,6 +209,14 @@ kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, uint64_t m, c
  * pass-start r, and the per-edge increments are summed -- the reference's
  * CDF_CliqueEnum (kCDensestNoAtom.c:270-295) with one thread per root edge. */
 #define KCLPP_SEQ_EDGE_STREAMS 1
+/* WAVES: the root vertices are split into waves by a fixed hash of their id,
+ * wave w = (uint32_t)(s * 2654435761) % W with W = the graph's
+ * kclpp_schedule.seq_waves (default 16); the waves run one after another and
+ * every root edge of a wave runs its chain from r as the earlier waves left
+ * it.  A block Gauss-Seidel ordering: the pass's load is balanced across
+ * waves, so the upper bound converges in several times fewer passes than
+ * with EDGE_STREAMS, at the cost of W ordered launches per pass. */
+#define KCLPP_SEQ_WAVES 2
 /* `passes` FRANK_WOLFE passes (CDF_CliqueEnum, kCDensestNoAtom.c:270-295) on
  * r (n entries, u64 as in kCDensestNoAtom.c:124). */
 kclpp_status kclpp_seq_passes(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t passes,

@@ -35,8 +35,9 @@ OK = 0
 ERR_INVALID, ERR_IO, ERR_NOMEM, ERR_CUDA, ERR_UNSUPPORTED, ERR_OVERFLOW, ERR_NODEVICE = 1, 2, 3, 4, 5, 6, 7
 MAX_K = 8
 SEQ_EDGE_STREAMS = 1
+SEQ_WAVES = 2
 TRIM_EXACT, TRIM_FAST = 0, 1
-GEN_CHUNG_LU, GEN_RMAT, GEN_ER, GEN_PLANTED = 1, 2, 3, 4
+GEN_CHUNG_LU, GEN_RMAT, GEN_ER, GEN_PLANTED, GEN_RMAT_PLANTED = 1, 2, 3, 4, 5
 
 
 class KclppError(RuntimeError):
@@ -75,7 +76,8 @@ TIER_NAMES = {0: "S", 1: "M", 2: "L"}
 
 class Schedule(C.Structure):
     _fields_ = [("tier_s_max", C.c_uint32), ("tier_s_max_seq", C.c_uint32), ("m_split1", C.c_uint32),
-                ("m_split2", C.c_uint32), ("steal_seq", C.c_int), ("steal_count", C.c_int)]
+                ("m_split2", C.c_uint32), ("steal_seq", C.c_int), ("steal_count", C.c_int),
+                ("seq_waves", C.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -318,6 +320,13 @@ def chung_lu(n: int, avg_degree: float, gamma: float, seed: int = 1) -> EdgeList
 
 def rmat(scale: int, edge_factor: int = 16, a=0.57, b=0.19, c=0.19, seed: int = 1) -> EdgeList:
     return generate(GEN_RMAT, scale=scale, edge_factor=edge_factor, a=a, b=b, c=c, seed=seed)
+
+
+def rmat_planted(scale: int, edge_factor: int, communities: int, comm_min: int, comm_max: int, p_in: float,
+                 a=0.57, b=0.19, c=0.19, seed: int = 1) -> EdgeList:
+    """RMAT graph plus planted G(n_c, p_in) communities (sizes log-uniform)."""
+    return generate(GEN_RMAT_PLANTED, scale=scale, edge_factor=edge_factor, a=a, b=b, c=c, communities=communities,
+                    comm_min=comm_min, comm_max=comm_max, p_in=p_in, seed=seed)
 
 
 def erdos_renyi(n: int, avg_degree: float, seed: int = 1) -> EdgeList:

@@ -74,7 +74,10 @@ struct kclpp_graph {
   int device = 0;
   HostDag dag;
   // Schedule knobs (tier bounds, stealing); the autotuner may change them.
-  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0};
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16};
+  // KCLPP_SEQ_WAVES: one Seq schedule per wave (roots grouped by a fixed hash).
+  std::vector<std::vector<TierInfo>> wave_tiers;
+  std::vector<uint32_t> wave_base;
   uint64_t *d_off = nullptr;
   uint32_t *d_cols = nullptr;
   uint32_t *d_src = nullptr;
@@ -181,6 +184,10 @@ static void shard_plan_host(uint32_t n, const uint64_t *off, uint32_t world, uin
   }
 }
 
+// Wave of a root for KCLPP_SEQ_WAVES: a fixed multiplicative hash, so roots of
+// similar work spread over the waves.
+static inline uint32_t wave_of(uint32_t s, uint32_t B) { return (uint32_t)(s * 2654435761u) % B; }
+
 // Root schedules: tiers by out-degree, descending work (out-degree, then id)
 // inside each tier; tier L first, then tier M from the largest roots down, so
 // that the longest CTAs start first.
@@ -230,6 +237,49 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
     if (sch == 0) g->num_roots = (uint32_t)all.size();
   }
   g->maxdeg = mx;
+  // Waves: the Seq roots again, grouped by wave_of(s); each group tiered as the
+  // Seq schedule is.
+  g->wave_tiers.clear();
+  g->wave_base.clear();
+  const uint32_t B = std::max<uint32_t>(g->sp.seq_waves, 1);
+  if (B > 1) {
+    std::vector<std::vector<uint32_t>> grp(B);
+    for (uint32_t s = 0; s < D.n; ++s) {
+      if (deg(s) == 0) continue;
+      if (g->shard_world > 1 && g->owner[s] != g->shard_rank) continue;
+      grp[wave_of(s, B)].push_back(s);
+    }
+    for (uint32_t w = 0; w < B; ++w) {
+      g->wave_base.push_back((uint32_t)all.size());
+      std::vector<uint32_t> tS, tM1, tM2, tM3, tL;
+      for (uint32_t s : grp[w]) {
+        const uint32_t d = deg(s);
+        if (d <= g->sp.tier_s_max_seq) tS.push_back(s);
+        else if (d <= g->sp.m_split1) tM1.push_back(s);
+        else if (d <= g->sp.m_split2) tM2.push_back(s);
+        else if (d <= kTierMMax) tM3.push_back(s);
+        else tL.push_back(s);
+      }
+      std::vector<TierInfo> tw;
+      auto addw = [&](std::vector<uint32_t> &v, int tier) {
+        if (v.empty()) return;
+        std::sort(v.begin(), v.end(), by_work);
+        TierInfo t;
+        t.tier = tier;
+        t.offset = (uint32_t)all.size();
+        t.count = (uint32_t)v.size();
+        t.dmax = deg(v.front());
+        all.insert(all.end(), v.begin(), v.end());
+        tw.push_back(t);
+      };
+      addw(tL, 2);
+      addw(tM3, 1);
+      addw(tM2, 1);
+      addw(tM1, 1);
+      addw(tS, 0);
+      g->wave_tiers.push_back(tw);
+    }
+  }
   KCL_TRY(dalloc(&g->d_roots, all.size()));
   if (!all.empty())
     KCL_CUDA(cudaMemcpyAsync(g->d_roots, all.data(), all.size() * 4, cudaMemcpyHostToDevice, c->stream));
@@ -293,9 +343,11 @@ struct Exec {
 
 // Launch every tier of one mode.
 static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev::PassArgs a,
-                              const Exec *ex = nullptr) {
+                              const Exec *ex = nullptr, int wave = -1) {
   const int sch = mode == dev::MODE_SEQ ? 1 : 0;
-  const std::vector<TierInfo> &tiers = g->tiers[sch];
+  const bool wv = mode == dev::MODE_SEQ && wave >= 0;
+  const std::vector<TierInfo> &tiers = wv ? g->wave_tiers[wave] : g->tiers[sch];
+  const uint32_t base = wv ? g->wave_base[wave] : g->sched_base[sch];
   if (tiers.empty()) return KCLPP_OK;
   const Exec E = ex ? *ex : Exec{c->stream, g->d_work, g->d_task};
   KCL_CUDA(cudaMemsetAsync(E.work, 0, 32 * sizeof(uint32_t), E.st));
@@ -313,7 +365,7 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     tl.num_roots = t.count;
     tl.dmax = t.dmax;
     tl.work = E.work + i;
-    tl.task_next = E.task + (t.offset - g->sched_base[sch]);
+    tl.task_next = E.task + (t.offset - base);
     // Work stealing pays off for the Seq chains (long, uneven root edges); the
     // counting kernels finish their roots quickly and by default do not steal.
     const bool steal = mode == dev::MODE_SEQ ? g->sp.steal_seq != 0 : g->sp.steal_count != 0;
@@ -344,9 +396,28 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
 }
 
 // ---- device-resident passes (enqueue only) ---------------------------------
+// One Seq pass from `in` into `out`.  KCLPP_SEQ_WAVES runs the waves in order,
+// each wave's root-edge streams starting from r after the previous waves; it
+// uses `in` as the second ping-pong buffer (its contents are not needed after
+// the pass).
 static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsigned long long *in,
-                                 unsigned long long *out, unsigned long long *cliques) {
+                                 unsigned long long *out, unsigned long long *cliques,
+                                 int det_mode = KCLPP_SEQ_EDGE_STREAMS) {
   const uint32_t n = g->dag.n;
+  if (det_mode == KCLPP_SEQ_WAVES && g->wave_tiers.size() > 1 && in != out) {
+    unsigned long long *src = const_cast<unsigned long long *>(in), *dst = out;
+    for (size_t w = 0; w < g->wave_tiers.size(); ++w) {
+      KCL_CUDA(cudaMemcpyAsync(dst, src, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->stream));
+      dev::PassArgs a{};
+      a.r_in = src;
+      a.out = dst;
+      a.cliques = cliques;
+      KCL_TRY(run_tiers(c, g, dev::MODE_SEQ, k, a, nullptr, (int)w));
+      std::swap(src, dst);
+    }
+    if (src != out) KCL_CUDA(cudaMemcpyAsync(out, src, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->stream));
+    return KCLPP_OK;
+  }
   if (in != out) KCL_CUDA(cudaMemcpyAsync(out, in, (size_t)n * 8, cudaMemcpyDeviceToDevice, c->stream));
   dev::PassArgs a{};
   a.r_in = in;
@@ -614,11 +685,12 @@ kclpp_status kclpp_count_cliques(kclpp_ctx *c, const kclpp_graph *gc, int k, uin
 }
 
 // ---- Seq --------------------------------------------------------------------------
-static kclpp_status seq_passes_on(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t passes, unsigned long long *r) {
+static kclpp_status seq_passes_on(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t passes, unsigned long long *r,
+                                  int det_mode = KCLPP_SEQ_EDGE_STREAMS) {
   // Ping-pong between r and the workspace; end with the result in r.
   unsigned long long *in = r, *out = g->d_b;
   for (uint32_t p = 0; p < passes; ++p) {
-    KCL_TRY(seq_pass_dev(c, g, k, in, out, nullptr));
+    KCL_TRY(seq_pass_dev(c, g, k, in, out, nullptr, det_mode));
     std::swap(in, out);
   }
   if (in != r) KCL_CUDA(cudaMemcpyAsync(r, in, (size_t)g->dag.n * 8, cudaMemcpyDeviceToDevice, c->stream));
@@ -629,22 +701,24 @@ kclpp_status kclpp_seq_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, ui
                                   uint64_t *r_dev) {
   if (!c || !gc || (!r_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
   KCL_TRY(check_k(k, 3));
-  if (det_mode != KCLPP_SEQ_EDGE_STREAMS) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
+    return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
   KCL_TRY(set_device(c));
-  return seq_passes_on(c, const_cast<kclpp_graph *>(gc), k, passes, (unsigned long long *)r_dev);
+  return seq_passes_on(c, const_cast<kclpp_graph *>(gc), k, passes, (unsigned long long *)r_dev, det_mode);
 }
 
 kclpp_status kclpp_seq_passes(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t passes, int det_mode,
                               uint64_t *r) {
   if (!c || !gc || (!r && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
   KCL_TRY(check_k(k, 3));
-  if (det_mode != KCLPP_SEQ_EDGE_STREAMS) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
+    return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
   const size_t bytes = (size_t)g->dag.n * 8;
   if (!bytes) return KCLPP_OK;
   KCL_CUDA(cudaMemcpyAsync(g->d_a, r, bytes, cudaMemcpyHostToDevice, c->stream));
-  KCL_TRY(seq_passes_on(c, g, k, passes, g->d_a));
+  KCL_TRY(seq_passes_on(c, g, k, passes, g->d_a, det_mode));
   KCL_CUDA(cudaMemcpyAsync(r, g->d_a, bytes, cudaMemcpyDeviceToHost, c->stream));
   return check_err(c);
 }
@@ -762,6 +836,8 @@ kclpp_status kclpp_sim_update_dev(kclpp_ctx *c, uint32_t n, uint32_t t, double *
 
 // ---- schedule knobs and the autotuner ----------------------------------------------------
 static kclpp_status check_schedule(const kclpp_schedule *sp) {
+  if (sp->seq_waves < 1 || sp->seq_waves > 1024)
+    return set_error(KCLPP_ERR_INVALID, "seq_waves must be in [1, 1024]");
   if (sp->tier_s_max > kTierSMax || sp->tier_s_max_seq > kTierSMax || sp->m_split1 < sp->tier_s_max ||
       sp->m_split1 < sp->tier_s_max_seq || sp->m_split2 < sp->m_split1 || sp->m_split2 > kTierMMax)
     return set_error(KCLPP_ERR_INVALID, "schedule bounds out of range (tier S <= %u <= split1 <= split2 <= %u)",
@@ -1250,7 +1326,8 @@ kclpp_status kclpp_seq_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t
                             uint64_t *r_out, kclpp_densest_info *infos, int max_infos, int *n_infos) {
   if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
   KCL_TRY(check_k(k, 3));
-  if (det_mode != KCLPP_SEQ_EDGE_STREAMS) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
+    return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
   const uint32_t n = g->dag.n;
@@ -1262,7 +1339,7 @@ kclpp_status kclpp_seq_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t
   if (n) KCL_CUDA(cudaMemsetAsync(dr, 0, (size_t)n * 8, c->stream));
   for (uint32_t T = 1, t = 1; T <= num_iter; T <<= 1) {
     if (T > t - 1) {
-      KCL_TRY(seq_passes_on(c, g, k, T - (t - 1), dr));
+      KCL_TRY(seq_passes_on(c, g, k, T - (t - 1), dr, det_mode));
       t = T + 1;
     }
     if (n) KCL_CUDA(cudaMemcpyAsync(r.data(), dr, (size_t)n * 8, cudaMemcpyDeviceToHost, c->stream));

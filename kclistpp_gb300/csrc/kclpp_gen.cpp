@@ -131,6 +131,26 @@ using namespace kclpp;
 
 extern "C" {
 
+static bool planted_ok(const kclpp_gen_params *p) {
+  return p->comm_min >= 2 && p->comm_max >= p->comm_min && p->p_in > 0 && p->p_in <= 1.0;
+}
+
+// Planted G(n_c, p_in) communities: disjoint slices of a fresh permutation,
+// sizes log-uniform in [comm_min, comm_max]; stops at the first that no longer fits.
+static void plant(uint32_t n, const kclpp_gen_params *p, SplitMix &rng, std::vector<uint64_t> &keys) {
+  auto members = permutation(n, rng);
+  uint64_t at = 0;
+  const double lmin = std::log((double)p->comm_min), lmax = std::log((double)p->comm_max);
+  for (uint32_t c = 0; c < p->communities; ++c) {
+    uint32_t sz = (uint32_t)std::llround(std::exp(lmin + (lmax - lmin) * rng.uniform()));
+    if (at + sz > n) break;
+    for (uint32_t i = 0; i < sz; ++i)
+      for (uint32_t j = i + 1; j < sz; ++j)
+        if (rng.uniform() < p->p_in) keys.push_back(pack(members[at + i], members[at + j]));
+    at += sz;
+  }
+}
+
 kclpp_status kclpp_generate(const kclpp_gen_params *p, kclpp_edge_list **out) {
   if (!p || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_generate: null argument");
   *out = nullptr;
@@ -157,9 +177,12 @@ kclpp_status kclpp_generate(const kclpp_gen_params *p, kclpp_edge_list **out) {
         }
         break;
       }
-      case KCLPP_GEN_RMAT: {
+      case KCLPP_GEN_RMAT:
+      case KCLPP_GEN_RMAT_PLANTED: {
         if (p->scale < 1 || p->scale > 31 || p->edge_factor < 1)
           return set_error(KCLPP_ERR_INVALID, "rmat: need 1 <= scale <= 31, edge_factor >= 1");
+        if (p->kind == KCLPP_GEN_RMAT_PLANTED && !planted_ok(p))
+          return set_error(KCLPP_ERR_INVALID, "rmat-planted: bad community parameters");
         const double a = p->a, ab = p->a + p->b, abc = p->a + p->b + p->c;
         if (!(a >= 0 && ab >= a && abc >= ab && abc <= 1.0))
           return set_error(KCLPP_ERR_INVALID, "rmat: bad quadrant probabilities");
@@ -183,26 +206,15 @@ kclpp_status kclpp_generate(const kclpp_gen_params *p, kclpp_edge_list **out) {
         // Scramble ids so that id order carries no degree information.
         auto perm = permutation(n, rng);
         for (auto &k : keys) k = pack(perm[(uint32_t)(k >> 32)], perm[(uint32_t)k]);
+        if (p->kind == KCLPP_GEN_RMAT_PLANTED) plant(n, p, rng, keys);
         break;
       }
       case KCLPP_GEN_PLANTED: {
-        if (n < 2 || !(p->avg_degree > 0) || !(p->gamma > 1.0) || p->comm_min < 2 ||
-            p->comm_max < p->comm_min || !(p->p_in > 0 && p->p_in <= 1.0))
+        if (n < 2 || !(p->avg_degree > 0) || !(p->gamma > 1.0) || !planted_ok(p))
           return set_error(KCLPP_ERR_INVALID, "planted: bad parameters");
         auto perm = permutation(n, rng);
         chung_lu_keys(n, p->avg_degree, p->gamma, rng, perm, keys);
-        // Communities are disjoint slices of a second permutation.
-        auto members = permutation(n, rng);
-        uint64_t at = 0;
-        const double lmin = std::log((double)p->comm_min), lmax = std::log((double)p->comm_max);
-        for (uint32_t c = 0; c < p->communities; ++c) {
-          uint32_t sz = (uint32_t)std::llround(std::exp(lmin + (lmax - lmin) * rng.uniform()));
-          if (at + sz > n) break;
-          for (uint32_t i = 0; i < sz; ++i)
-            for (uint32_t j = i + 1; j < sz; ++j)
-              if (rng.uniform() < p->p_in) keys.push_back(pack(members[at + i], members[at + j]));
-          at += sz;
-        }
+        plant(n, p, rng, keys);
         break;
       }
       default:

@@ -22,7 +22,7 @@ import time
 import numpy as np
 
 from . import (Context, DensestInfo, EdgeList, Graph, _check, _lib, build_graph, extract_densest_seq,
-               extract_densest_seq_warm, seq_passes, seq_passes_dev)
+               extract_densest_seq_warm, seq_passes, seq_passes_dev, SEQ_EDGE_STREAMS)
 
 NPARAMS = 64 * 4 + 64 + 64 + 1
 
@@ -119,8 +119,9 @@ class WarmModel:
 
 
 def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, model: WarmModel | None = None,
-                t0: float = 16.0, trace: bool = False) -> dict:
-    """Run Seq passes (per-root-edge streams) until (ub - density) / ub <= gap.
+                t0: float = 16.0, trace: bool = False, det_mode: int = SEQ_EDGE_STREAMS) -> dict:
+    """Run Seq passes (per-root-edge streams, or waves with det_mode=SEQ_WAVES)
+    until (ub - density) / ub <= gap.
 
     Zero start when model is None; otherwise start at r0 = model.start_r(g, t0)
     (the features, the inference and r0 are inside the timed region).  With
@@ -140,7 +141,7 @@ def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, mode
     p = 0
     hist = []
     while p < max_passes:
-        seq_passes_dev(g, k, 1, r_dev.data_ptr())
+        seq_passes_dev(g, k, 1, r_dev.data_ptr(), det_mode)
         g.ctx.synchronize()
         p += 1
         r = r_dev.cpu().numpy().view(np.uint64)

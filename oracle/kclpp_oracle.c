@@ -567,6 +567,23 @@ void orc_sim_counts_masked(const orc_graph *g, int k, const double *rho, const u
   visit_all_masked(g, k, p, g->n, cnt, threads, 1, root_mask);
 }
 
+/* Wave ordering: root vertices grouped by (uint32)(s * 2654435761) % waves;
+ * the waves run in order, each one's root-edge streams starting from r as the
+ * earlier waves left it. */
+int orc_seq_pass_waves(const orc_graph *g, int k, uint64_t *rho, uint32_t waves, int threads) {
+  if (k < 3 || k >= ORC_MAXK || waves == 0) return -1;
+  uint8_t *mask = (uint8_t *)xmalloc((size_t)g->n + 1);
+  uint64_t *delta = (uint64_t *)xmalloc(((size_t)g->n + 1) * sizeof(uint64_t));
+  for (uint32_t w = 0; w < waves; ++w) {
+    for (uint32_t s = 0; s < g->n; ++s) mask[s] = ((uint32_t)(s * 2654435761u) % waves) == w;
+    orc_seq_delta_masked(g, k, rho, mask, threads, delta);
+    for (uint32_t x = 0; x < g->n; ++x) rho[x] += delta[x];
+  }
+  free(mask);
+  free(delta);
+  return 0;
+}
+
 int orc_seq_pass(const orc_graph *g, int k, uint64_t *rho, int mode, int threads) {
   if (k < 3 || k >= ORC_MAXK) return -1;
   seq_pass_impl(g, k, rho, mode, threads, 1);

@@ -71,6 +71,8 @@ void orc_sort_by_r_u64(uint32_t n, const uint64_t *rho, uint32_t *reordered);
 /* Sampled pass for the timed CPU baseline: every stride-th root edge; returns cliques visited. */
 uint64_t orc_seq_pass_sample(const orc_graph *g, int k, uint64_t *rho, int mode, int threads, uint64_t stride);
 
+/* Wave ordering of a Seq pass (the library's KCLPP_SEQ_WAVES). */
+int orc_seq_pass_waves(const orc_graph *g, int k, uint64_t *rho, uint32_t waves, int threads);
 /* One shard of a split pass: only root edges whose source is marked. */
 int orc_seq_delta_masked(const orc_graph *g, int k, const uint64_t *rho, const uint8_t *root_mask, int threads,
                          uint64_t *delta);

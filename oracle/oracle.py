@@ -86,6 +86,7 @@ def lib() -> C.CDLL:
             "orc_free_trim": (None, [C.POINTER(OrcTrim)]),
             "orc_seq_main": (C.c_int, [G, C.c_int, C.c_uint32, C.c_int, C.c_int, u64p, C.POINTER(OrcInfo), C.c_int]),
             "orc_sim_main": (C.c_int, [G, C.c_int, C.c_uint32, C.c_int, f64p, C.POINTER(OrcInfo), C.c_int]),
+            "orc_seq_pass_waves": (C.c_int, [G, C.c_int, u64p, C.c_uint32, C.c_int]),
             "orc_seq_delta_masked": (C.c_int, [G, C.c_int, u64p, C.POINTER(C.c_uint8), C.c_int, u64p]),
             "orc_sim_counts_masked": (None, [G, C.c_int, f64p, C.POINTER(C.c_uint8), C.c_int, u64p]),
             "orc_wtime": (C.c_double, []),
@@ -194,6 +195,12 @@ class Graph:
         tent = np.zeros(self.n + 1, dtype=np.uint64)
         lib().orc_seq_pava(self._g, k, _p(level, C.c_uint32), _p(tent, C.c_uint64), threads)
         return tent[: self.n]
+
+    def seq_pass_waves(self, k: int, r: np.ndarray, waves: int, threads: int = 1) -> np.ndarray:
+        r = np.array(r, dtype=np.uint64, copy=True)
+        if lib().orc_seq_pass_waves(self._g, k, _p(r, C.c_uint64), waves, threads) != 0:
+            raise ValueError("oracle: unsupported k")
+        return r
 
     def seq_delta_masked(self, k: int, r: np.ndarray, mask: np.ndarray, threads: int = 1) -> np.ndarray:
         """Increments of one shard's root edges (EDGE_STREAMS order)."""

@@ -152,6 +152,27 @@ def test_tiers_seq_pass_from_nonzero_r(ctx, name, k):
 
 
 @pytest.mark.parametrize("name,k", TIER_CASES)
+@pytest.mark.parametrize("waves", [16, 5])
+def test_tiers_seq_waves(ctx, name, k, waves):
+    """Wave-ordered passes: each wave's chains start from r as the earlier
+    waves left it, so the result depends on the wave hash and the ordering of
+    waves -- both must match the oracle's restatement bit for bit."""
+    P = TIERS[name]
+    g = dev_graph(ctx, P)
+    sp = K.get_schedule(g)
+    sp.seq_waves = waves
+    K.set_schedule(g, sp)
+    og = O.Graph(P)
+    r0 = np.random.default_rng(200 + k).integers(0, 4, size=g.n, dtype=np.uint64) * np.uint64(1000)
+    r = K.seq_passes(g, k, 2, r0, det_mode=K.SEQ_WAVES)
+    ro = og.seq_pass_waves(k, og.seq_pass_waves(k, r0, waves, THREADS), waves, THREADS)
+    assert np.array_equal(r, ro)
+    # a pass adds exactly one unit per k-clique
+    tot, _ = og.count_cliques(k)
+    assert int((r - r0).sum()) == 2 * tot
+
+
+@pytest.mark.parametrize("name,k", TIER_CASES)
 def test_tiers_sim_counts_with_ties(ctx, name, k):
     P = TIERS[name]
     g = dev_graph(ctx, P)

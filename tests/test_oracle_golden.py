@@ -80,3 +80,26 @@ def test_known_answers():
         assert infos[-1].n == 10 and infos[-1].cliques == comb(10, k)
     star = O.Graph(G.pairs("kat_star"))
     assert star.count_cliques(3)[0] == 0
+
+
+@pytest.mark.parametrize("name,k,T", G.case_ks())
+def test_seq_waves_restatement(name, k, T):
+    """The wave ordering has no reference counterpart; pin it to what it is
+    built from.  One wave is exactly the per-root-edge-stream pass (which the
+    reference pins above); with several waves each wave's increment is the
+    masked per-root-edge delta from r as the earlier waves left it, and every
+    pass still hands out one unit per k-clique."""
+    g = O.Graph(G.pairs(name))
+    tot, _ = g.count_cliques(k)
+    rng = np.random.default_rng(k)
+    r0 = rng.integers(0, 3, size=g.n, dtype=np.uint64)
+    assert np.array_equal(g.seq_pass_waves(k, r0, 1), g.seq_pass(k, r0, mode=O.SEQ_EDGE_STREAMS))
+    for waves in (3, 16):
+        r = r0.copy()
+        ids = np.arange(g.n, dtype=np.uint64)
+        wave = ((ids * np.uint64(2654435761)) & np.uint64(0xFFFFFFFF)) % np.uint64(waves)
+        for w in range(waves):
+            r = r + g.seq_delta_masked(k, r, (wave == w).astype(np.uint8))
+        got = g.seq_pass_waves(k, r0, waves)
+        assert np.array_equal(got, r)
+        assert int((got - r0).sum()) == tot
