@@ -144,6 +144,10 @@ typedef struct {
   int steal_seq;            /* work stealing in the Seq kernel                                    */
   int steal_count;          /* work stealing in the counting kernels                              */
   uint32_t seq_waves;       /* waves of KCLPP_SEQ_WAVES, 1..1024 (default 16)                     */
+  uint32_t seq_warps[4];    /* Seq kernel, warps per CTA of the M1 (<= m_split1), M2 (<= m_split2), */
+                            /* M3 (<= 1024) and L root groups: 8, 12, 16, 20 or 24; 0 = the width  */
+                            /* that keeps the most warps resident per SM                           */
+  int concurrent_tiers;     /* launch a pass's root groups on forked streams (default 1)          */
 } kclpp_schedule;
 kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp);
 kclpp_status kclpp_graph_set_schedule(kclpp_ctx *ctx, kclpp_graph *g, const kclpp_schedule *sp);

@@ -77,10 +77,15 @@ TIER_NAMES = {0: "S", 1: "M", 2: "L"}
 class Schedule(C.Structure):
     _fields_ = [("tier_s_max", C.c_uint32), ("tier_s_max_seq", C.c_uint32), ("m_split1", C.c_uint32),
                 ("m_split2", C.c_uint32), ("steal_seq", C.c_int), ("steal_count", C.c_int),
-                ("seq_waves", C.c_uint32)]
+                ("seq_waves", C.c_uint32), ("seq_warps", C.c_uint32 * 4),
+                ("concurrent_tiers", C.c_int)]
+
+    def __init__(self, **kw):
+        arr = {f: t for f, t in self._fields_ if issubclass(t, C.Array)}
+        super().__init__(**{f: (arr[f](*v) if f in arr and not isinstance(v, C.Array) else v) for f, v in kw.items()})
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        return {f: (list(getattr(self, f)) if issubclass(t, C.Array) else getattr(self, f)) for f, t in self._fields_}
 
 
 class TuneResult(C.Structure):

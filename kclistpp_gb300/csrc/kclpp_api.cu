@@ -50,6 +50,10 @@ struct kclpp_ctx {
   uint32_t *d_err = nullptr;
   uint64_t launches = 0;
   bool profile = false;
+  // Side streams for the concurrent launch of a pass's root groups, forked
+  // from and joined back into `stream` with events.
+  cudaStream_t side[4] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[4] = {};
   std::vector<PendingTime> pending;
   std::vector<cudaEvent_t> event_pool;
 };
@@ -67,6 +71,7 @@ static cudaEvent_t take_event(kclpp_ctx *c) {
 
 struct TierInfo {
   int tier;
+  int bucket;  // 0..3: the M1, M2, M3 and L root groups (kclpp_schedule.seq_warps); -1: tier S
   uint32_t offset, count, dmax;
 };
 
@@ -74,7 +79,7 @@ struct kclpp_graph {
   int device = 0;
   HostDag dag;
   // Schedule knobs (tier bounds, stealing); the autotuner may change them.
-  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16};
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1};
   // KCLPP_SEQ_WAVES: one Seq schedule per wave (roots grouped by a fixed hash).
   std::vector<std::vector<TierInfo>> wave_tiers;
   std::vector<uint32_t> wave_base;
@@ -218,22 +223,23 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
     any_l |= !tL.empty();
     g->sched_base[sch] = (uint32_t)all.size();
     g->tiers[sch].clear();
-    auto add = [&](std::vector<uint32_t> &v, int tier) {
+    auto add = [&](std::vector<uint32_t> &v, int tier, int bucket) {
       if (v.empty()) return;
       std::sort(v.begin(), v.end(), by_work);
       TierInfo t;
       t.tier = tier;
+      t.bucket = bucket;
       t.offset = (uint32_t)all.size();
       t.count = (uint32_t)v.size();
       t.dmax = deg(v.front());
       all.insert(all.end(), v.begin(), v.end());
       g->tiers[sch].push_back(t);
     };
-    add(tL, 2);
-    add(tM3, 1);
-    add(tM2, 1);
-    add(tM1, 1);
-    add(tS, 0);
+    add(tL, 2, 3);
+    add(tM3, 1, 2);
+    add(tM2, 1, 1);
+    add(tM1, 1, 0);
+    add(tS, 0, -1);
     if (sch == 0) g->num_roots = (uint32_t)all.size();
   }
   g->maxdeg = mx;
@@ -261,22 +267,23 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
         else tL.push_back(s);
       }
       std::vector<TierInfo> tw;
-      auto addw = [&](std::vector<uint32_t> &v, int tier) {
+      auto addw = [&](std::vector<uint32_t> &v, int tier, int bucket) {
         if (v.empty()) return;
         std::sort(v.begin(), v.end(), by_work);
         TierInfo t;
         t.tier = tier;
+        t.bucket = bucket;
         t.offset = (uint32_t)all.size();
         t.count = (uint32_t)v.size();
         t.dmax = deg(v.front());
         all.insert(all.end(), v.begin(), v.end());
         tw.push_back(t);
       };
-      addw(tL, 2);
-      addw(tM3, 1);
-      addw(tM2, 1);
-      addw(tM1, 1);
-      addw(tS, 0);
+      addw(tL, 2, 3);
+      addw(tM3, 1, 2);
+      addw(tM2, 1, 1);
+      addw(tM1, 1, 0);
+      addw(tS, 0, -1);
       g->wave_tiers.push_back(tw);
     }
   }
@@ -357,8 +364,18 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
   a.err = c->d_err;
   a.slab = g->d_slab;
   a.slab_words = g->slab_words;
+  // Root groups of one pass are independent (they read the pass-start vector
+  // and add into the output), so they may run side by side: the later groups
+  // fill the SMs that the first one's tail leaves idle.
+  const int nside =
+      (!ex && g->sp.concurrent_tiers && tiers.size() > 1) ? (int)std::min<size_t>(tiers.size() - 1, 4) : 0;
+  if (nside) {
+    KCL_CUDA(cudaEventRecord(c->fork_ev, E.st));
+    for (int j = 0; j < nside; ++j) KCL_CUDA(cudaStreamWaitEvent(c->side[j], c->fork_ev, 0));
+  }
   for (size_t i = 0; i < tiers.size(); ++i) {
     const TierInfo &t = tiers[i];
+    const cudaStream_t ls = (nside && i > 0) ? c->side[(i - 1) % nside] : E.st;
     TierLaunch tl;
     tl.tier = t.tier;
     tl.roots = g->d_roots + t.offset;
@@ -372,25 +389,30 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     tl.steal_cursor = steal ? E.work + 16 + i : nullptr;
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
+    tl.seq_warps = t.bucket >= 0 ? (int)g->sp.seq_warps[t.bucket] : 0;
     cudaError_t e = cudaSuccess;
     PendingTime pt{mode, t.tier, t.dmax, nullptr, nullptr};
     const bool prof = c->profile && !ex;
     if (prof) {
       pt.a = take_event(c);
       pt.b = take_event(c);
-      if (pt.a) cudaEventRecord(pt.a, E.st);
+      if (pt.a) cudaEventRecord(pt.a, ls);
     }
-    if (mode == dev::MODE_COUNT) e = launch_count(k, tl, a, E.st);
-    else if (mode == dev::MODE_ORDER) e = launch_order(k, tl, a, E.st);
-    else e = launch_seq(k, tl, a, E.st);
+    if (mode == dev::MODE_COUNT) e = launch_count(k, tl, a, ls);
+    else if (mode == dev::MODE_ORDER) e = launch_order(k, tl, a, ls);
+    else e = launch_seq(k, tl, a, ls);
     if (prof && pt.a && pt.b) {
-      cudaEventRecord(pt.b, E.st);
+      cudaEventRecord(pt.b, ls);
       c->pending.push_back(pt);
     }
     if (e != cudaSuccess)
       return set_error(KCLPP_ERR_CUDA, "kernel launch (mode %d, tier %d, k %d): %s", mode, t.tier, k,
                        cudaGetErrorString(e));
     c->launches++;
+  }
+  for (int j = 0; j < nside; ++j) {
+    KCL_CUDA(cudaEventRecord(c->join_ev[j], c->side[j]));
+    KCL_CUDA(cudaStreamWaitEvent(E.st, c->join_ev[j], 0));
   }
   return KCLPP_OK;
 }
@@ -519,6 +541,11 @@ kclpp_status kclpp_create(int device, void *stream, kclpp_ctx **out) {
     KCL_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     c->own_stream = true;
   }
+  for (int i = 0; i < 4; ++i) {
+    KCL_CUDA(cudaStreamCreateWithFlags(&c->side[i], cudaStreamNonBlocking));
+    KCL_CUDA(cudaEventCreateWithFlags(&c->join_ev[i], cudaEventDisableTiming));
+  }
+  KCL_CUDA(cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming));
   KCL_CUDA(cudaMalloc((void **)&c->d_err, sizeof(uint32_t)));
   KCL_CUDA(cudaMemsetAsync(c->d_err, 0, sizeof(uint32_t), c->stream));
   KCL_CUDA(cudaStreamSynchronize(c->stream));
@@ -533,6 +560,11 @@ kclpp_status kclpp_destroy(kclpp_ctx *c) {
   for (auto &p : c->pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   for (auto e : c->event_pool) cudaEventDestroy(e);
   cudaFree(c->d_err);
+  for (int i = 0; i < 4; ++i) {
+    if (c->side[i]) cudaStreamDestroy(c->side[i]);
+    if (c->join_ev[i]) cudaEventDestroy(c->join_ev[i]);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
   return KCLPP_OK;
@@ -836,6 +868,11 @@ kclpp_status kclpp_sim_update_dev(kclpp_ctx *c, uint32_t n, uint32_t t, double *
 
 // ---- schedule knobs and the autotuner ----------------------------------------------------
 static kclpp_status check_schedule(const kclpp_schedule *sp) {
+  for (int i = 0; i < 4; ++i) {
+    const uint32_t w = sp->seq_warps[i];
+    if (w != 0 && (w < 8 || w > (uint32_t)kWarpsMSeqMax || w % 4))
+      return set_error(KCLPP_ERR_INVALID, "seq_warps entries must be 0 or one of 8, 12, 16, 20, 24");
+  }
   if (sp->seq_waves < 1 || sp->seq_waves > 1024)
     return set_error(KCLPP_ERR_INVALID, "seq_waves must be in [1, 1024]");
   if (sp->tier_s_max > kTierSMax || sp->tier_s_max_seq > kTierSMax || sp->m_split1 < sp->tier_s_max ||
@@ -884,6 +921,36 @@ static kclpp_status time_pass(kclpp_ctx *c, kclpp_graph *g, int k, int mode, flo
   KCL_CUDA(cudaEventElapsedTime(ms, e0, e1));
   c->event_pool.push_back(e0);
   c->event_pool.push_back(e1);
+  return check_err(c);
+}
+
+// Per-launch times of one Seq pass (after a warm-up pass), in launch order:
+// the per-launch events of the profiler, kept apart from the caller's.
+static kclpp_status time_seq_tiers(kclpp_ctx *c, kclpp_graph *g, int k, std::vector<float> &ms) {
+  const size_t bytes = (size_t)g->dag.n * 8;
+  std::vector<PendingTime> saved;
+  saved.swap(c->pending);
+  const bool was = c->profile;
+  kclpp_status st = KCLPP_OK;
+  for (int rep = 0; rep < 2 && st == KCLPP_OK; ++rep) {
+    for (auto &p : c->pending) { c->event_pool.push_back(p.a); c->event_pool.push_back(p.b); }
+    c->pending.clear();
+    c->profile = rep == 1;
+    if (cudaMemsetAsync(g->d_a, 0, bytes, c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "memset failed");
+    if (st == KCLPP_OK) st = seq_pass_dev(c, g, k, g->d_a, g->d_b, nullptr);
+  }
+  c->profile = was;
+  if (st == KCLPP_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "sync failed");
+  ms.clear();
+  for (auto &p : c->pending) {
+    float t = 0.f;
+    if (st == KCLPP_OK) cudaEventElapsedTime(&t, p.a, p.b);
+    ms.push_back(t);
+    c->event_pool.push_back(p.a);
+    c->event_pool.push_back(p.b);
+  }
+  c->pending.swap(saved);
+  if (st != KCLPP_OK) return st;
   return check_err(c);
 }
 
@@ -936,11 +1003,47 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
     KCL_TRY(time_pass(c, g, k, mode, &ms));
     if (ms < best) { best = ms; best_sp = x; }
   }
+  if (mode == dev::MODE_SEQ) {
+    // Warps per CTA, chosen per root group: the groups run as separate
+    // launches, so each one's width is tuned on its own launch time.
+    const uint32_t widths[5] = {8, 12, 16, 20, 24};
+    float bt[4] = {1e30f, 1e30f, 1e30f, 1e30f};
+    kclpp_schedule tuned = best_sp;
+    bool any = false;
+    for (uint32_t w : widths) {
+      kclpp_schedule x = best_sp;
+      x.concurrent_tiers = 0;  // each group's own launch time
+      for (int b = 0; b < 4; ++b) x.seq_warps[b] = w;
+      KCL_TRY(kclpp_graph_set_schedule(c, g, &x));
+      std::vector<float> ms;
+      KCL_TRY(time_seq_tiers(c, g, k, ms));
+      const std::vector<TierInfo> &tiers = g->tiers[1];
+      for (size_t i = 0; i < tiers.size() && i < ms.size(); ++i) {
+        const int b = tiers[i].bucket;
+        if (b >= 0 && ms[i] < bt[b]) { bt[b] = ms[i]; tuned.seq_warps[b] = w; any = true; }
+      }
+    }
+    if (any) {
+      KCL_TRY(kclpp_graph_set_schedule(c, g, &tuned));
+      float ms = 0.f;
+      KCL_TRY(time_pass(c, g, k, mode, &ms));
+      if (ms < best) { best = ms; best_sp = tuned; }
+    }
+  }
+  {
+    // Root groups side by side or one after another.
+    kclpp_schedule x = best_sp;
+    x.concurrent_tiers = !best_sp.concurrent_tiers;
+    KCL_TRY(kclpp_graph_set_schedule(c, g, &x));
+    float ms = 0.f;
+    KCL_TRY(time_pass(c, g, k, mode, &ms));
+    if (ms < best) { best = ms; best_sp = x; }
+  }
   KCL_TRY(kclpp_graph_set_schedule(c, g, &best_sp));
   out->best = best_sp;
   out->best_ms = best;
   out->default_ms = def;
-  out->candidates = (int)cand.size() + 1;
+  out->candidates = (int)cand.size() + 2 + (mode == dev::MODE_SEQ ? 6 : 0);
   return KCLPP_OK;
 }
 

@@ -298,13 +298,22 @@ struct Bits {
   uint32_t w[WPL];
 };
 
-template <int WPL>
+// Seq rows hold only the ids below their own (N+(x) lies below x): row i
+// keeps ceil(i / 32) words, packed one after another from word tri_off(i),
+// which halves the bitmap and leaves shared memory for more stream warps.
+__host__ __device__ __forceinline__ uint32_t tri_off(uint32_t i) {
+  const uint32_t a = i >> 5, b = i & 31;
+  return 16u * a * (a - (a > 0)) + 31u * a + (b ? a + (b - 1) * (a + 1) : 0u);
+}
+template <int WPL, bool TRI = false>
 __device__ __forceinline__ Bits<WPL> load_row(const uint32_t *rows, int r, int W, int lane) {
   Bits<WPL> b;
+  const size_t o = TRI ? (size_t)tri_off((uint32_t)r) : (size_t)r * W;
+  const int n = TRI ? (r + 31) >> 5 : W;
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
     const int w = lane + 32 * q;
-    b.w[q] = w < W ? rows[(size_t)r * W + w] : 0u;
+    b.w[q] = w < n ? rows[o + w] : 0u;
   }
   return b;
 }
@@ -391,7 +400,8 @@ __host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, boo
   const size_t W = (dmax + 31) / 32;
   size_t at = 0;
   L.list = at; at = align16(at + (size_t)dmax * 4);
-  L.rows = at; if (rows_in_smem) at = align16(at + (size_t)dmax * W * 4);
+  L.rows = at;
+  if (rows_in_smem) at = align16(at + (mode == MODE_SEQ ? (size_t)tri_off(dmax) : (size_t)dmax * W) * 4);
   L.base = at; if (mode != MODE_COUNT) at = align16(at + (size_t)(dmax + 1) * 8);
   L.acc = at; if (mode == MODE_SEQ) at = align16(at + (size_t)(dmax + 1) * 8);
   L.rank = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
@@ -476,7 +486,7 @@ __device__ __forceinline__ uint64_t seq_warp(const Bits<WPL> &P, int g, const ui
     uint64_t c = 0;                                          // kCDensestNoAtom.c:173-188
     for_each_bit<WPL>(P, [&](int u) {
       const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
-      const Bits<WPL> V = band(P, load_row<WPL>(rows, u, W, lane));
+      const Bits<WPL> V = band(P, load_row<WPL, true>(rows, u, W, lane));
       c += chain_warp<WPL>(V, g2, base, dl, buf, lane, err);
     });
     return c;
@@ -486,7 +496,7 @@ __device__ __forceinline__ uint64_t seq_warp(const Bits<WPL> &P, int g, const ui
     uint64_t c = 0;
     for_each_bit<WPL>(P, [&](int u) {
       const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
-      const Bits<WPL> Q = band(P, load_row<WPL>(rows, u, W, lane));
+      const Bits<WPL> Q = band(P, load_row<WPL, true>(rows, u, W, lane));
       c += seq_warp<L - 1, WPL>(Q, g2, rows, W, base, dl, buf, lane, err);
     });
     return c;
@@ -517,7 +527,7 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
 template <int MODE, int K, int WPL, bool ROWS_IN_SMEM, bool IDENT = false>
 __global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int NW = warps_m<MODE>();
+  const int NW = MODE == MODE_SEQ ? (int)(blockDim.x >> 5) : warps_m<MODE>();
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int dmax = (int)a.dmax;
   const LayoutM lay = layout_m(MODE, a.dmax, NW, ROWS_IN_SMEM);
@@ -577,8 +587,9 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a
       continue;
     }
     const int W = (d + 31) >> 5;
+    const int row_words = MODE == MODE_SEQ ? (int)tri_off((uint32_t)d) : d * W;
     for (int i = tid; i < d; i += NW * 32) list[i] = a.cols[o + i];
-    for (int i = tid; i < d * W; i += NW * 32) rows[i] = 0;
+    for (int i = tid; i < row_words; i += NW * 32) rows[i] = 0;
     if constexpr (MODE == MODE_ORDER) {
       for (int i = tid; i < d; i += NW * 32) base[i] = vertex_key(a, a.cols[o + i]);
       if (tid == 0) base[d] = vertex_key(a, s);
@@ -620,7 +631,7 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a
           const int j = lower_bound_u32(list, i, y);
           if (list[j] != y) continue;
           if constexpr (MODE == MODE_SEQ) {
-            atomicOr(&rows[(size_t)i * W + (j >> 5)], 1u << (j & 31));
+            atomicOr(&rows[(size_t)tri_off((uint32_t)i) + (j >> 5)], 1u << (j & 31));
           } else if constexpr (MODE == MODE_COUNT) {
             atomicOr(&rows[(size_t)i * W + (j >> 5)], 1u << (j & 31));
             atomicOr(&rows[(size_t)j * W + (i >> 5)], 1u << (i & 31));
@@ -640,7 +651,7 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a
         q = __shfl_sync(KCL_FULL, q, 0);
         if (q >= d) break;
         const int j = d - 1 - q;  // larger candidate sets first
-        const Bits<WPL> C = load_row<WPL>(rows, j, W, lane);
+        const Bits<WPL> C = load_row<WPL, true>(rows, j, W, lane);
         if (!any_bits<WPL>(C)) continue;
         const int g0 = base[j] < base[d] ? j : d;  // kCDensestNoAtom.c:287
         visited += seq_warp<K - 2, WPL>(C, g0, rows, W, base, dl, buf, lane, a.err);
@@ -725,9 +736,14 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a
 struct LaunchCache {
   std::mutex mu;
   int attr_bytes = -1;
-  size_t occ_smem[32];  // fixed storage: launching never touches the heap
-  int occ_ctas[32];
+  size_t occ_smem[64];  // fixed storage: launching never touches the heap
+  int occ_threads[64];
+  int occ_ctas[64];
   int nocc = 0;
+  // Seq tiers M / L: chosen warps per CTA by (out-degree bound, requested width).
+  uint32_t nw_dmax[32];
+  int nw_req[32], nw_val[32];
+  int nnw = 0;
 };
 
 template <typename Fn>
@@ -739,15 +755,49 @@ static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int
     lc.attr_bytes = (int)smem;
   }
   for (int i = 0; i < lc.nocc; ++i)
-    if (lc.occ_smem[i] == smem) { *per_sm = lc.occ_ctas[i]; return cudaSuccess; }
+    if (lc.occ_smem[i] == smem && lc.occ_threads[i] == threads) { *per_sm = lc.occ_ctas[i]; return cudaSuccess; }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess || nb < 1) nb = 1;
-  if (lc.nocc < 32) {
+  if (lc.nocc < 64) {
     lc.occ_smem[lc.nocc] = smem;
+    lc.occ_threads[lc.nocc] = threads;
     lc.occ_ctas[lc.nocc] = nb;
     ++lc.nocc;
   }
   *per_sm = nb;
+  return cudaSuccess;
+}
+
+// Warps per CTA of a Seq tier M / L launch: `req` when nonzero, else the
+// width in 8..kWarpsMSeqMax (steps of 4) that keeps the most warps resident
+// per SM at this out-degree bound (ties: the narrower, i.e. more CTAs).
+template <typename Fn>
+static cudaError_t pick_seq_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
+  using namespace dev;
+  {
+    std::lock_guard<std::mutex> g(lc.mu);
+    for (int i = 0; i < lc.nnw; ++i)
+      if (lc.nw_dmax[i] == dmax && lc.nw_req[i] == req) { *nw = lc.nw_val[i]; return cudaSuccess; }
+  }
+  int best = 0, best_warps = -1;
+  for (int w = 8; w <= kWarpsMSeqMax; w += 4) {
+    if (req > 0 && w != req) continue;
+    const size_t sm = layout_m(MODE_SEQ, dmax, w, rows_in_smem).total;
+    if (sm > 227 * 1024) continue;
+    int per_sm = 0;
+    cudaError_t e = prepare(fn, lc, w * 32, sm, &per_sm);
+    if (e != cudaSuccess) return e;
+    if (per_sm * w > best_warps) { best_warps = per_sm * w; best = w; }
+  }
+  if (best == 0) best = 8;
+  std::lock_guard<std::mutex> g(lc.mu);
+  if (lc.nnw < 32) {
+    lc.nw_dmax[lc.nnw] = dmax;
+    lc.nw_req[lc.nnw] = req;
+    lc.nw_val[lc.nnw] = best;
+    ++lc.nnw;
+  }
+  *nw = best;
   return cudaSuccess;
 }
 
@@ -784,22 +834,27 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
     fn<<<persistent_grid(per_sm, t, kWarpsS, false), kWarpsS * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
-  constexpr int NW = warps_m<MODE>();
   if (t.tier == 1) {
     static LaunchCache lc;
-    const size_t sm = layout_m(MODE, t.dmax, NW, true).total;
     auto fn = tier_m_kernel<MODE, K, 1, true>;
-    cudaError_t e = prepare(fn, lc, NW * 32, sm, &per_sm);
+    int nw = warps_m<MODE>();
+    cudaError_t e = MODE == MODE_SEQ ? pick_seq_warps(fn, lc, t.dmax, true, t.seq_warps, &nw) : cudaSuccess;
     if (e != cudaSuccess) return e;
-    fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), NW * 32, sm, st>>>(a);
+    const size_t sm = layout_m(MODE, t.dmax, nw, true).total;
+    e = prepare(fn, lc, nw * 32, sm, &per_sm);
+    if (e != cudaSuccess) return e;
+    fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), nw * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
   static LaunchCache lc;
-  const size_t sm = layout_m(MODE, t.dmax, NW, false).total;
   auto fn = tier_m_kernel<MODE, K, 2, false>;
-  cudaError_t e = prepare(fn, lc, NW * 32, sm, &per_sm);
+  int nw = warps_m<MODE>();
+  cudaError_t e = MODE == MODE_SEQ ? pick_seq_warps(fn, lc, t.dmax, false, t.seq_warps, &nw) : cudaSuccess;
   if (e != cudaSuccess) return e;
-  fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), NW * 32, sm, st>>>(a);
+  const size_t sm = layout_m(MODE, t.dmax, nw, false).total;
+  e = prepare(fn, lc, nw * 32, sm, &per_sm);
+  if (e != cudaSuccess) return e;
+  fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), nw * 32, sm, st>>>(a);
   return cudaGetLastError();
 }
 
