@@ -148,6 +148,8 @@ typedef struct {
                             /* M3 (<= 1024) and L root groups: 8, 12, 16, 20 or 24; 0 = the width  */
                             /* that keeps the most warps resident per SM                           */
   int concurrent_tiers;     /* launch a pass's root groups on forked streams (default 1)          */
+  uint32_t count_warps[4];  /* the counting / Sim kernels' widths of the same four groups:         */
+                            /* 8, 16, 24 or 32; 0 = the most resident warps per SM                 */
 } kclpp_schedule;
 kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp);
 kclpp_status kclpp_graph_set_schedule(kclpp_ctx *ctx, kclpp_graph *g, const kclpp_schedule *sp);

@@ -79,7 +79,7 @@ struct kclpp_graph {
   int device = 0;
   HostDag dag;
   // Schedule knobs (tier bounds, stealing); the autotuner may change them.
-  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1};
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1, {0, 0, 0, 0}};
   // KCLPP_SEQ_WAVES: one Seq schedule per wave (roots grouped by a fixed hash).
   std::vector<std::vector<TierInfo>> wave_tiers;
   std::vector<uint32_t> wave_base;
@@ -389,7 +389,7 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     tl.steal_cursor = steal ? E.work + 16 + i : nullptr;
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
-    tl.seq_warps = t.bucket >= 0 ? (int)g->sp.seq_warps[t.bucket] : 0;
+    tl.warps = t.bucket < 0 ? 0 : (int)(mode == dev::MODE_SEQ ? g->sp.seq_warps[t.bucket] : g->sp.count_warps[t.bucket]);
     cudaError_t e = cudaSuccess;
     PendingTime pt{mode, t.tier, t.dmax, nullptr, nullptr};
     const bool prof = c->profile && !ex;
@@ -872,6 +872,9 @@ static kclpp_status check_schedule(const kclpp_schedule *sp) {
     const uint32_t w = sp->seq_warps[i];
     if (w != 0 && (w < 8 || w > (uint32_t)kWarpsMSeqMax || w % 4))
       return set_error(KCLPP_ERR_INVALID, "seq_warps entries must be 0 or one of 8, 12, 16, 20, 24");
+    const uint32_t v = sp->count_warps[i];
+    if (v != 0 && (v < 8 || v > (uint32_t)kWarpsMMax || v % 8))
+      return set_error(KCLPP_ERR_INVALID, "count_warps entries must be 0 or one of 8, 16, 24, 32");
   }
   if (sp->seq_waves < 1 || sp->seq_waves > 1024)
     return set_error(KCLPP_ERR_INVALID, "seq_waves must be in [1, 1024]");
@@ -924,9 +927,9 @@ static kclpp_status time_pass(kclpp_ctx *c, kclpp_graph *g, int k, int mode, flo
   return check_err(c);
 }
 
-// Per-launch times of one Seq pass (after a warm-up pass), in launch order:
-// the per-launch events of the profiler, kept apart from the caller's.
-static kclpp_status time_seq_tiers(kclpp_ctx *c, kclpp_graph *g, int k, std::vector<float> &ms) {
+// Per-launch times of one pass of `mode` (after a warm-up pass), in launch
+// order: the per-launch events of the profiler, kept apart from the caller's.
+static kclpp_status time_tiers(kclpp_ctx *c, kclpp_graph *g, int k, int mode, std::vector<float> &ms) {
   const size_t bytes = (size_t)g->dag.n * 8;
   std::vector<PendingTime> saved;
   saved.swap(c->pending);
@@ -936,8 +939,13 @@ static kclpp_status time_seq_tiers(kclpp_ctx *c, kclpp_graph *g, int k, std::vec
     for (auto &p : c->pending) { c->event_pool.push_back(p.a); c->event_pool.push_back(p.b); }
     c->pending.clear();
     c->profile = rep == 1;
-    if (cudaMemsetAsync(g->d_a, 0, bytes, c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "memset failed");
-    if (st == KCLPP_OK) st = seq_pass_dev(c, g, k, g->d_a, g->d_b, nullptr);
+    if (mode == dev::MODE_SEQ) {
+      if (cudaMemsetAsync(g->d_a, 0, bytes, c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "memset failed");
+      if (st == KCLPP_OK) st = seq_pass_dev(c, g, k, g->d_a, g->d_b, nullptr);
+    } else {
+      if (cudaMemsetAsync(g->d_rho, 0, bytes, c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "memset failed");
+      if (st == KCLPP_OK) st = sim_counts_dev(c, g, k, g->d_rho, g->d_a);
+    }
   }
   c->profile = was;
   if (st == KCLPP_OK && cudaStreamSynchronize(c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "sync failed");
@@ -1003,24 +1011,32 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
     KCL_TRY(time_pass(c, g, k, mode, &ms));
     if (ms < best) { best = ms; best_sp = x; }
   }
-  if (mode == dev::MODE_SEQ) {
+  {
     // Warps per CTA, chosen per root group: the groups run as separate
     // launches, so each one's width is tuned on its own launch time.
-    const uint32_t widths[5] = {8, 12, 16, 20, 24};
+    const bool sq = mode == dev::MODE_SEQ;
+    const uint32_t seq_w[5] = {8, 12, 16, 20, 24}, cnt_w[4] = {8, 16, 24, 32};
+    const uint32_t *widths = sq ? seq_w : cnt_w;
+    const int nwid = sq ? 5 : 4;
     float bt[4] = {1e30f, 1e30f, 1e30f, 1e30f};
     kclpp_schedule tuned = best_sp;
     bool any = false;
-    for (uint32_t w : widths) {
+    for (int wi = 0; wi < nwid; ++wi) {
+      const uint32_t w = widths[wi];
       kclpp_schedule x = best_sp;
       x.concurrent_tiers = 0;  // each group's own launch time
-      for (int b = 0; b < 4; ++b) x.seq_warps[b] = w;
+      for (int b = 0; b < 4; ++b) (sq ? x.seq_warps : x.count_warps)[b] = w;
       KCL_TRY(kclpp_graph_set_schedule(c, g, &x));
       std::vector<float> ms;
-      KCL_TRY(time_seq_tiers(c, g, k, ms));
-      const std::vector<TierInfo> &tiers = g->tiers[1];
+      KCL_TRY(time_tiers(c, g, k, mode, ms));
+      const std::vector<TierInfo> &tiers = g->tiers[sq ? 1 : 0];
       for (size_t i = 0; i < tiers.size() && i < ms.size(); ++i) {
         const int b = tiers[i].bucket;
-        if (b >= 0 && ms[i] < bt[b]) { bt[b] = ms[i]; tuned.seq_warps[b] = w; any = true; }
+        if (b >= 0 && ms[i] < bt[b]) {
+          bt[b] = ms[i];
+          (sq ? tuned.seq_warps : tuned.count_warps)[b] = w;
+          any = true;
+        }
       }
     }
     if (any) {
@@ -1043,7 +1059,7 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
   out->best = best_sp;
   out->best_ms = best;
   out->default_ms = def;
-  out->candidates = (int)cand.size() + 2 + (mode == dev::MODE_SEQ ? 6 : 0);
+  out->candidates = (int)cand.size() + 2 + (mode == dev::MODE_SEQ ? 6 : 5);
   return KCLPP_OK;
 }
 

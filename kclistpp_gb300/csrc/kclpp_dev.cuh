@@ -102,22 +102,22 @@ struct TierLaunch {
   uint32_t *steal_cursor;
   int num_sms;
   int max_grid;      // upper bound on CTAs (tier L: CTAs the row slab holds)
-  int seq_warps;     // Seq tiers M / L: warps per CTA (0 = the most resident warps)
+  int warps;         // tiers M / L: warps per CTA (0 = the most resident warps)
 };
 cudaError_t launch_count(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st);
 cudaError_t launch_order(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st);
 cudaError_t launch_seq(int k, const TierLaunch &t, dev::PassArgs a, cudaStream_t st);
-// Threads per CTA for a tier.  Tier M / L CTAs of the Seq kernel are wider
-// and sized at launch: their warps each run one root-edge stream with a
-// per-warp delta array, so the width that keeps the most warps resident
-// depends on the launch's out-degree bound (kWarpsMSeqMax is the upper limit;
-// the counting kernels' warps share one bitmap per CTA).
+// Threads per CTA.  Tier S: kWarpsS warps.  Tiers M / L are sized at launch
+// (the schedule's width, or the one that keeps the most warps resident at the
+// launch's out-degree bound): the Seq kernel's warps each run a root-edge
+// stream with a per-warp delta array (8..kWarpsMSeqMax warps); the counting
+// kernels' warps share one bitmap per CTA (8..kWarpsMMax warps).
 constexpr int kWarpsS = 4;
 constexpr int kWarpsM = 8;
-constexpr int kWarpsMSeq = 12;
+constexpr int kWarpsMMax = 32;
 constexpr int kWarpsMSeqMax = 24;
 template <int MODE>
-constexpr int warps_m() { return MODE == dev::MODE_SEQ ? kWarpsMSeqMax : kWarpsM; }
+constexpr int warps_m() { return MODE == dev::MODE_SEQ ? kWarpsMSeqMax : kWarpsMMax; }
 // Tier bounds on a root's out-degree.  The Seq kernel keeps only the smallest
 // roots on tier S (a lane runs a whole root-edge stream there, which is slow
 // on dense roots); the counting kernels use tier S up to 64.

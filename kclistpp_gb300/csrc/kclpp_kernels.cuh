@@ -524,10 +524,17 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
   return UINT32_MAX;
 }
 
+// Register budget of a tier M / L kernel, as CTAs of the widest launch that
+// must fit one SM: two for k <= 5 (the Seq kernel then keeps <= 42 registers a
+// thread, the counting kernels <= 32, so that two wide CTAs are resident),
+// one for the deeper recursions of k >= 6, which would otherwise spill.
+template <int MODE, int K>
+constexpr int min_ctas_m() { return K <= 5 ? 2 : 1; }
+
 template <int MODE, int K, int WPL, bool ROWS_IN_SMEM, bool IDENT = false>
-__global__ void __launch_bounds__(warps_m<MODE>() * 32) tier_m_kernel(PassArgs a) {
+__global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) tier_m_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int NW = MODE == MODE_SEQ ? (int)(blockDim.x >> 5) : warps_m<MODE>();
+  const int NW = (int)(blockDim.x >> 5);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int dmax = (int)a.dmax;
   const LayoutM lay = layout_m(MODE, a.dmax, NW, ROWS_IN_SMEM);
@@ -768,21 +775,23 @@ static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int
   return cudaSuccess;
 }
 
-// Warps per CTA of a Seq tier M / L launch: `req` when nonzero, else the
-// width in 8..kWarpsMSeqMax (steps of 4) that keeps the most warps resident
-// per SM at this out-degree bound (ties: the narrower, i.e. more CTAs).
-template <typename Fn>
-static cudaError_t pick_seq_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
+// Warps per CTA of a tier M / L launch: `req` when nonzero, else the width
+// that keeps the most warps resident per SM at this out-degree bound (ties:
+// the narrower, i.e. more CTAs).  Seq: 8..24 in steps of 4; the counting
+// kernels: 8..32 in steps of 8.
+template <int MODE, typename Fn>
+static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
   using namespace dev;
+  constexpr int lo = 8, hi = warps_m<MODE>(), step = MODE == MODE_SEQ ? 4 : 8;
   {
     std::lock_guard<std::mutex> g(lc.mu);
     for (int i = 0; i < lc.nnw; ++i)
       if (lc.nw_dmax[i] == dmax && lc.nw_req[i] == req) { *nw = lc.nw_val[i]; return cudaSuccess; }
   }
   int best = 0, best_warps = -1;
-  for (int w = 8; w <= kWarpsMSeqMax; w += 4) {
+  for (int w = lo; w <= hi; w += step) {
     if (req > 0 && w != req) continue;
-    const size_t sm = layout_m(MODE_SEQ, dmax, w, rows_in_smem).total;
+    const size_t sm = layout_m(MODE, dmax, w, rows_in_smem).total;
     if (sm > 227 * 1024) continue;
     int per_sm = 0;
     cudaError_t e = prepare(fn, lc, w * 32, sm, &per_sm);
@@ -837,8 +846,8 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
   if (t.tier == 1) {
     static LaunchCache lc;
     auto fn = tier_m_kernel<MODE, K, 1, true>;
-    int nw = warps_m<MODE>();
-    cudaError_t e = MODE == MODE_SEQ ? pick_seq_warps(fn, lc, t.dmax, true, t.seq_warps, &nw) : cudaSuccess;
+    int nw = kWarpsM;
+    cudaError_t e = pick_warps<MODE>(fn, lc, t.dmax, true, t.warps, &nw);
     if (e != cudaSuccess) return e;
     const size_t sm = layout_m(MODE, t.dmax, nw, true).total;
     e = prepare(fn, lc, nw * 32, sm, &per_sm);
@@ -848,8 +857,8 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
   }
   static LaunchCache lc;
   auto fn = tier_m_kernel<MODE, K, 2, false>;
-  int nw = warps_m<MODE>();
-  cudaError_t e = MODE == MODE_SEQ ? pick_seq_warps(fn, lc, t.dmax, false, t.seq_warps, &nw) : cudaSuccess;
+  int nw = kWarpsM;
+  cudaError_t e = pick_warps<MODE>(fn, lc, t.dmax, false, t.warps, &nw);
   if (e != cudaSuccess) return e;
   const size_t sm = layout_m(MODE, t.dmax, nw, false).total;
   e = prepare(fn, lc, nw * 32, sm, &per_sm);
