@@ -423,7 +423,7 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
 // uses `in` as the second ping-pong buffer (its contents are not needed after
 // the pass).
 static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsigned long long *in,
-                                 unsigned long long *out, unsigned long long *cliques,
+                                 unsigned long long *out,
                                  int det_mode = KCLPP_SEQ_EDGE_STREAMS) {
   const uint32_t n = g->dag.n;
   if (det_mode == KCLPP_SEQ_WAVES && g->wave_tiers.size() > 1 && in != out) {
@@ -433,7 +433,6 @@ static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsi
       dev::PassArgs a{};
       a.r_in = src;
       a.out = dst;
-      a.cliques = cliques;
       KCL_TRY(run_tiers(c, g, dev::MODE_SEQ, k, a, nullptr, (int)w));
       std::swap(src, dst);
     }
@@ -444,7 +443,6 @@ static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsi
   dev::PassArgs a{};
   a.r_in = in;
   a.out = out;
-  a.cliques = cliques;
   return run_tiers(c, g, dev::MODE_SEQ, k, a);
 }
 
@@ -722,7 +720,7 @@ static kclpp_status seq_passes_on(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t 
   // Ping-pong between r and the workspace; end with the result in r.
   unsigned long long *in = r, *out = g->d_b;
   for (uint32_t p = 0; p < passes; ++p) {
-    KCL_TRY(seq_pass_dev(c, g, k, in, out, nullptr, det_mode));
+    KCL_TRY(seq_pass_dev(c, g, k, in, out, det_mode));
     std::swap(in, out);
   }
   if (in != r) KCL_CUDA(cudaMemcpyAsync(r, in, (size_t)g->dag.n * 8, cudaMemcpyDeviceToDevice, c->stream));
@@ -912,7 +910,7 @@ static kclpp_status time_pass(kclpp_ctx *c, kclpp_graph *g, int k, int mode, flo
     if (mode == dev::MODE_SEQ) {
       KCL_CUDA(cudaMemsetAsync(g->d_a, 0, bytes, c->stream));
       KCL_CUDA(cudaEventRecord(e0, c->stream));
-      KCL_TRY(seq_pass_dev(c, g, k, g->d_a, g->d_b, nullptr));
+      KCL_TRY(seq_pass_dev(c, g, k, g->d_a, g->d_b));
     } else {
       KCL_CUDA(cudaMemsetAsync(g->d_rho, 0, bytes, c->stream));
       KCL_CUDA(cudaEventRecord(e0, c->stream));
@@ -941,7 +939,7 @@ static kclpp_status time_tiers(kclpp_ctx *c, kclpp_graph *g, int k, int mode, st
     c->profile = rep == 1;
     if (mode == dev::MODE_SEQ) {
       if (cudaMemsetAsync(g->d_a, 0, bytes, c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "memset failed");
-      if (st == KCLPP_OK) st = seq_pass_dev(c, g, k, g->d_a, g->d_b, nullptr);
+      if (st == KCLPP_OK) st = seq_pass_dev(c, g, k, g->d_a, g->d_b);
     } else {
       if (cudaMemsetAsync(g->d_rho, 0, bytes, c->stream) != cudaSuccess) st = set_error(KCLPP_ERR_CUDA, "memset failed");
       if (st == KCLPP_OK) st = sim_counts_dev(c, g, k, g->d_rho, g->d_a);

@@ -49,7 +49,6 @@ struct PassArgs {
   const uint32_t *level;          // KEY_LEVEL
   unsigned long long *out;        // COUNT: nck; ORDER: per-vertex count; SEQ: r after the pass
   const unsigned long long *r_in; // SEQ: r at the start of the pass
-  unsigned long long *cliques;    // optional: cliques visited (SEQ), nullptr to skip
   uint32_t *slab;                 // tier L: per-CTA row storage in global memory
   uint64_t slab_words;            // words per CTA in slab
   uint32_t deg_lo, deg_hi;        // id-order schedules: out-degree window of this launch

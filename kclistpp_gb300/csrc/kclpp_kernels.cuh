@@ -149,7 +149,6 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
     for (int i = lane; i <= kSMaxD; i += 32) sm.acc[i] = 0;
     for (int i = 0; i < kSDl; ++i) sm.dl[lane * kSDl + i] = 0;
   }
-  unsigned long long visited = 0;
   __syncwarp();
   for (;;) {
     uint32_t idx = 0;
@@ -236,7 +235,7 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
         const unsigned long long C = sm.rows[j];
         if (!C) continue;
         const int g0 = sm.base[j] < sm.base[d] ? j : d;  // kCDensestNoAtom.c:287
-        visited += seq64<K - 2>(C, g0, sm.rows, sm.base, dl);
+        seq64<K - 2>(C, g0, sm.rows, sm.base, dl);
         // Close the stream: its increments fell on {s, t} ∪ C.
         unsigned long long it = C;
         while (it) {
@@ -282,12 +281,6 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
     }
     __syncwarp();
   }
-  if constexpr (MODE == MODE_SEQ) {
-    if (a.cliques) {
-      visited = warp_sum(visited);
-      if (lane == 0 && visited) atomicAdd(a.cliques, visited);
-    }
-  }
 }
 
 // ========================================================================
@@ -299,17 +292,17 @@ struct Bits {
 };
 
 // Seq rows hold only the ids below their own (N+(x) lies below x): row i
-// keeps ceil(i / 32) words, packed one after another from word tri_off(i),
+// keeps (i >> 5) + 1 words, packed one after another from word tri_off(i),
 // which halves the bitmap and leaves shared memory for more stream warps.
 __host__ __device__ __forceinline__ uint32_t tri_off(uint32_t i) {
   const uint32_t a = i >> 5, b = i & 31;
-  return 16u * a * (a - (a > 0)) + 31u * a + (b ? a + (b - 1) * (a + 1) : 0u);
+  return i + a * (16u * a + b - 16u * (a > 0));
 }
 template <int WPL, bool TRI = false>
 __device__ __forceinline__ Bits<WPL> load_row(const uint32_t *rows, int r, int W, int lane) {
   Bits<WPL> b;
   const size_t o = TRI ? (size_t)tri_off((uint32_t)r) : (size_t)r * W;
-  const int n = TRI ? (r + 31) >> 5 : W;
+  const int n = TRI ? (r >> 5) + 1 : W;
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
     const int w = lane + 32 * q;
@@ -392,7 +385,7 @@ __device__ __forceinline__ uint64_t cnt_warp(const Bits<WPL> &P, const uint32_t 
 // Shared-memory layout of a tier M / L CTA (dmax = largest out-degree the
 // launch allows, NW warps).  Tier L keeps `rows` in a global slab instead.
 struct LayoutM {
-  size_t list, rows, base, acc, rank, inv, dl, buf, total;
+  size_t list, rows, base, base32, acc, rank, inv, dl, total;
 };
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 __host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, bool rows_in_smem) {
@@ -403,29 +396,47 @@ __host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, boo
   L.rows = at;
   if (rows_in_smem) at = align16(at + (mode == MODE_SEQ ? (size_t)tri_off(dmax) : (size_t)dmax * W) * 4);
   L.base = at; if (mode != MODE_COUNT) at = align16(at + (size_t)(dmax + 1) * 8);
+  L.base32 = at; if (mode == MODE_SEQ) at = align16(at + (size_t)(dmax + 1) * 4);
   L.acc = at; if (mode == MODE_SEQ) at = align16(at + (size_t)(dmax + 1) * 8);
   L.rank = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
   L.inv = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
   L.dl = at; if (mode == MODE_SEQ) at = align16(at + (size_t)nw * (dmax + 1) * 4);
-  L.buf = at; if (mode == MODE_SEQ) at = align16(at + (size_t)nw * dmax * 2);
   L.total = at;
   return L;
 }
 
-// The Seq chain over V (last level) from prefix argmin g, 32 candidates at a time.
+// The Seq chain over V (the last level), one 32-bit word of V at a time: lane
+// b stands for candidate 32 * word + b.  c is the current value of the prefix
+// argmin (kCDensestNoAtom.c:162-171 and 180-186: each clique goes to the
+// candidate w when r[w] < c, strict, else to the prefix argmin, whose value
+// then grows by one).  Inside a word the chain is resolved by a ballot fixed
+// point on 32-bit distances: rel = r[w] - c (-1 when r[w] < c, which always
+// takes the clique), and candidate i falls to the prefix iff rel_i >= the
+// number of earlier candidates of the word that fell to it.  Returns the
+// prefix argmin's new value.
 //
-// Compaction: the candidates are written to the warp's buffer in ascending
-// order one nonzero word at a time, a lane per bit (position = candidates
-// before the word + set bits of the word below the lane), so no lane loops
-// over its own bits.  Each chunk of 32 then resolves the chain by the ballot
-// fixed point on 32-bit distances: rel = cur[v] - c (clamped; -1 when cur[v]
-// is below c, which always succeeds), and candidate i fails iff rel_i >= the
-// failures before it in the chunk.
-template <int WPL>
-__device__ __forceinline__ uint32_t chain_warp(const Bits<WPL> &V, int g, const unsigned long long *base,
-                                               uint32_t *dl, uint16_t *buf, int lane, uint32_t *err) {
+// T is the value type: unsigned long long (pass-start r as is; distances
+// clamped to 2^31 - 1), or uint32_t when the root's values were stored
+// relative to their minimum and every value the stream can reach stays below
+// 2^31, so that a plain 32-bit difference is the distance.
+//
+// Vertex x's delta dl[x] is only ever read and written by lane x & 31 (here,
+// and for the argmin updates of seq_rec), so the chains need no warp barrier.
+template <typename T>
+__device__ __forceinline__ int distance(T av, T c) {
+  if constexpr (sizeof(T) == 4) {
+    return (int)(av - c);
+  } else {
+    if (av < c) return -1;
+    const T dd = av - c;
+    return dd > 0x7fffffffull ? 0x7fffffff : (int)dd;
+  }
+}
+
+template <int WPL, bool OVF, typename T>
+__device__ __forceinline__ T chain_words(const Bits<WPL> &V, T c, const T *base, uint32_t *dl, int lane,
+                                         uint32_t *err) {
   const uint32_t lt = lanemask_lt();
-  uint32_t total = 0;
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
     uint32_t nz = __ballot_sync(KCL_FULL, V.w[q] != 0);
@@ -433,74 +444,116 @@ __device__ __forceinline__ uint32_t chain_warp(const Bits<WPL> &V, int g, const 
       const int L = __ffs(nz) - 1;
       nz &= nz - 1;
       const uint32_t word = __shfl_sync(KCL_FULL, V.w[q], L);
-      if ((word >> lane) & 1u) buf[total + __popc(word & lt)] = (uint16_t)(((L + 32 * q) << 5) | lane);
-      total += (uint32_t)__popc(word);
-    }
-  }
-  if (total == 0) return 0;
-  __syncwarp();
-  const unsigned long long c0 = base[g] + dl[g];
-  unsigned long long c = c0;
-  for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-    const uint32_t idx = b0 + lane;
-    const bool valid = idx < total;
-    const int v = valid ? buf[idx] : 0;
-    int rel = -1;
-    if (valid) {
-      const unsigned long long av = base[v] + dl[v];
-      if (av >= c) {
-        const unsigned long long dd = av - c;
-        rel = dd > 0x7fffffffull ? 0x7fffffff : (int)dd;
+      const bool valid = (word >> lane) & 1u;
+      const int v = ((L + 32 * q) << 5) | lane;
+      int rel = -1;
+      uint32_t dv = 0;
+      if (valid) {
+        dv = dl[v];
+        rel = distance<T>(base[v] + dv, c);
       }
+      uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
+      for (int r = 0; r < 33; ++r) {
+        const uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+        if (m2 == m) break;
+        m = m2;
+      }
+      if (valid && !((m >> lane) & 1u)) {
+        if (OVF && dv == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
+        dl[v] = dv + 1u;
+      }
+      c += (T)__popc(m);
     }
-    uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
-    for (int r = 0; r < 33; ++r) {
-      const int f = __popc(m & lt);
-      const uint32_t m2 = __ballot_sync(KCL_FULL, rel >= f);
-      if (m2 == m) break;
-      m = m2;
-    }
-    if (valid && !((m >> lane) & 1u)) {
-      if (dl[v] == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
-      dl[v] += 1u;
-    }
-    c += (unsigned long long)__popc(m);
   }
-  __syncwarp();
-  if (lane == 0) {
-    const unsigned long long nd = (unsigned long long)dl[g] + (c - c0);
-    if (nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
-    dl[g] = (uint32_t)nd;
-  }
-  __syncwarp();
-  return total;
+  return c;
 }
 
-template <int L, int WPL>
-__device__ __forceinline__ uint64_t seq_warp(const Bits<WPL> &P, int g, const uint32_t *rows, int W,
-                                             const unsigned long long *base, uint32_t *dl, uint16_t *buf,
-                                             int lane, uint32_t *err) {
+// Current value of vertex x (pass-start r plus this stream's delta), read by
+// the lane that owns dl[x] and broadcast.
+template <typename T>
+__device__ __forceinline__ T value_of(int x, const T *base, const uint32_t *dl, int lane) {
+  T v = 0;
+  if ((x & 31) == lane) v = base[x] + dl[x];
+  return __shfl_sync(KCL_FULL, v, x & 31);
+}
+
+// Level L of a root-edge stream over candidates P with prefix argmin g of
+// current value cg (kCDensestNoAtom.c:173-188 for L = 2, 237-259 above).
+// Returns g's new value; the argmin of a deeper prefix, when it is u, is
+// written back to dl[u] by u's lane.
+template <int L, int WPL, bool OVF, typename T>
+__device__ __forceinline__ T seq_rec(const Bits<WPL> &P, T cg, const uint32_t *rows, const T *base, uint32_t *dl,
+                                     int lane, uint32_t *err) {
   if constexpr (L == 1) {
-    return chain_warp<WPL>(P, g, base, dl, buf, lane, err);  // kCDensestNoAtom.c:162-171
-  } else if constexpr (L == 2) {
-    uint64_t c = 0;                                          // kCDensestNoAtom.c:173-188
-    for_each_bit<WPL>(P, [&](int u) {
-      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
-      const Bits<WPL> V = band(P, load_row<WPL, true>(rows, u, W, lane));
-      c += chain_warp<WPL>(V, g2, base, dl, buf, lane, err);
-    });
-    return c;
+    return chain_words<WPL, OVF, T>(P, cg, base, dl, lane, err);
   } else {
-    int pc = warp_sum(popc_lane(P));                          // kCDensestNoAtom.c:218
-    if (pc < L) return 0;
-    uint64_t c = 0;
+    if constexpr (L >= 3) {
+      const int pc = warp_sum(popc_lane(P));  // kCDensestNoAtom.c:218
+      if (pc < L) return cg;
+    }
     for_each_bit<WPL>(P, [&](int u) {
-      const int g2 = (base[u] + dl[u]) < (base[g] + dl[g]) ? u : g;
-      const Bits<WPL> Q = band(P, load_row<WPL, true>(rows, u, W, lane));
-      c += seq_warp<L - 1, WPL>(Q, g2, rows, W, base, dl, buf, lane, err);
+      const T vu = value_of<T>(u, base, dl, lane);
+      const bool take = vu < cg;  // strict: ties stay with the earlier argmin
+      const Bits<WPL> Q = band(P, load_row<WPL, true>(rows, u, 0, lane));
+      const T c0 = take ? vu : cg;
+      const T c1 = seq_rec<L - 1, WPL, OVF, T>(Q, c0, rows, base, dl, lane, err);
+      if (take) {
+        if (lane == (u & 31)) {
+          const unsigned long long nd = (unsigned long long)dl[u] + (unsigned long long)(c1 - c0);
+          if (OVF && nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
+          dl[u] = (uint32_t)nd;
+        }
+      } else {
+        cg = c1;
+      }
     });
-    return c;
+    return cg;
   }
+}
+
+// Every root-edge stream of the current root, the warp taking streams from
+// the root's shared counter (largest candidate sets first); increments go to
+// the CTA's acc[] (kCDensestNoAtom.c:270-295 per root edge).
+template <int K, int WPL, typename T>
+__device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_t *rows, const T *base,
+                                            uint32_t *dl, unsigned long long *acc, int lane, uint32_t *err) {
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = (int)atomicAdd(next, 1u);
+    q = __shfl_sync(KCL_FULL, q, 0);
+    if (q >= d) break;
+    const int j = d - 1 - q;
+    const Bits<WPL> C = load_row<WPL, true>(rows, j, 0, lane);
+    if (!any_bits<WPL>(C)) continue;
+    const int g0 = base[j] < base[d] ? j : d;  // kCDensestNoAtom.c:287
+    const T c0 = base[g0];
+    const T c1 = seq_rec<K - 2, WPL, (K >= 6), T>(C, c0, rows, base, dl, lane, err);
+    // Close the stream: its increments fell on C (each member's delta held
+    // by its own lane) and on the edge's argmin g0 (held in c1).
+#pragma unroll
+    for (int qq = 0; qq < WPL; ++qq) {
+      uint32_t nz = __ballot_sync(KCL_FULL, C.w[qq] != 0);
+      while (nz) {
+        const int L = __ffs(nz) - 1;
+        nz &= nz - 1;
+        const uint32_t word = __shfl_sync(KCL_FULL, C.w[qq], L);
+        if ((word >> lane) & 1u) {
+          const int i = ((L + 32 * qq) << 5) | lane;
+          const uint32_t v = dl[i];
+          if (v) { atomicAdd(&acc[i], (unsigned long long)v); dl[i] = 0; }
+        }
+      }
+    }
+    if (lane == 0 && c1 != c0) atomicAdd(&acc[g0], (unsigned long long)(c1 - c0));
+  }
+}
+
+// Largest increment one vertex can take within a stream of a root with out-
+// degree d: the (k-2)-subsets of a candidate set of at most d - 1 members.
+__device__ __forceinline__ unsigned long long stream_bound(int K, int d) {
+  unsigned long long b = 1;
+  for (int i = 0; i < K - 2; ++i) b = b * (unsigned long long)(d - 1 - i) / (unsigned long long)(i + 1);
+  return b;
 }
 
 // Work stealing: once the root list is exhausted, an idle CTA joins a root
@@ -525,11 +578,12 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
 }
 
 // Register budget of a tier M / L kernel, as CTAs of the widest launch that
-// must fit one SM: two for k <= 5 (the Seq kernel then keeps <= 42 registers a
-// thread, the counting kernels <= 32, so that two wide CTAs are resident),
-// one for the deeper recursions of k >= 6, which would otherwise spill.
+// must fit one SM: two for the shallow recursions (the Seq kernel then keeps
+// <= 42 registers a thread at k = 3, 4, the counting kernels <= 32 at k <= 5,
+// so that two wide CTAs are resident), one for the deeper ones, which would
+// otherwise spill.
 template <int MODE, int K>
-constexpr int min_ctas_m() { return K <= 5 ? 2 : 1; }
+constexpr int min_ctas_m() { return K <= (MODE == MODE_SEQ ? 4 : 5) ? 2 : 1; }
 
 template <int MODE, int K, int WPL, bool ROWS_IN_SMEM, bool IDENT = false>
 __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) tier_m_kernel(PassArgs a) {
@@ -546,17 +600,18 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
   uint16_t *rank = reinterpret_cast<uint16_t *>(smem_raw + lay.rank);
   uint16_t *inv = reinterpret_cast<uint16_t *>(smem_raw + lay.inv);
   uint32_t *dl = reinterpret_cast<uint32_t *>(smem_raw + lay.dl) + (size_t)wid * (dmax + 1);
-  uint16_t *buf = reinterpret_cast<uint16_t *>(smem_raw + lay.buf) + (size_t)wid * dmax;
 
   __shared__ uint32_t s_idx;
   __shared__ int s_tau;
   __shared__ unsigned long long s_sum;
+  __shared__ unsigned long long s_min, s_max;
+  __shared__ bool s_rel32;
+  uint32_t *base32 = reinterpret_cast<uint32_t *>(smem_raw + lay.base32);
 
   if constexpr (MODE == MODE_SEQ) {
     for (int i = tid; i <= dmax; i += NW * 32) acc[i] = 0;
     for (int i = lane; i <= dmax; i += 32) dl[i] = 0;
   }
-  unsigned long long visited = 0;
   bool stealing = false;  // read by thread 0 only
   __syncthreads();
   for (;;) {
@@ -603,9 +658,36 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
     }
     if constexpr (MODE == MODE_SEQ) {
       for (int i = tid; i < d; i += NW * 32) base[i] = a.r_in[a.cols[o + i]];
-      if (tid == 0) base[d] = a.r_in[s];
+      if (tid == 0) {
+        base[d] = a.r_in[s];
+        s_min = ~0ull;
+        s_max = 0;
+      }
     }
     __syncthreads();
+    if constexpr (MODE == MODE_SEQ) {
+      // 32-bit values relative to the root's minimum when every value a stream
+      // can reach stays below 2^31 (k <= 5 only: deeper streams can exceed it).
+      if constexpr (K <= 5) {
+        unsigned long long lo = ~0ull, hi = 0;
+        for (int i = tid; i <= d; i += NW * 32) {
+          const unsigned long long v = base[i];
+          lo = v < lo ? v : lo;
+          hi = v > hi ? v : hi;
+        }
+        atomicMin(&s_min, lo);
+        atomicMax(&s_max, hi);
+        __syncthreads();
+        const unsigned long long mn = s_min;
+        const bool r32 = s_max - mn + stream_bound(K, d) < 0x7fffffffull;
+        if (r32)
+          for (int i = tid; i <= d; i += NW * 32) base32[i] = (uint32_t)(base[i] - mn);
+        if (tid == 0) s_rel32 = r32;
+      } else {
+        if (tid == 0) s_rel32 = false;
+      }
+      __syncthreads();
+    }
     if constexpr (MODE == MODE_ORDER) {
       const unsigned long long ks = base[d];
       int t = 0;
@@ -652,34 +734,11 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
       __syncthreads();
     }
     if constexpr (MODE == MODE_SEQ) {
-      for (;;) {
-        int q = 0;
-        if (lane == 0) q = (int)atomicAdd(next, 1u);
-        q = __shfl_sync(KCL_FULL, q, 0);
-        if (q >= d) break;
-        const int j = d - 1 - q;  // larger candidate sets first
-        const Bits<WPL> C = load_row<WPL, true>(rows, j, W, lane);
-        if (!any_bits<WPL>(C)) continue;
-        const int g0 = base[j] < base[d] ? j : d;  // kCDensestNoAtom.c:287
-        visited += seq_warp<K - 2, WPL>(C, g0, rows, W, base, dl, buf, lane, a.err);
-        // Close the stream: its increments fell on {s, t} ∪ C.
-#pragma unroll
-        for (int qq = 0; qq < WPL; ++qq) {
-          uint32_t w = C.w[qq];
-          while (w) {
-            const int b = __ffs(w) - 1;
-            w &= w - 1;
-            const int i = (lane + 32 * qq) * 32 + b;
-            const uint32_t v = dl[i];
-            if (v) { atomicAdd(&acc[i], (unsigned long long)v); dl[i] = 0; }
-          }
-        }
-        if (lane == 0) {
-          if (dl[j]) { atomicAdd(&acc[j], (unsigned long long)dl[j]); dl[j] = 0; }
-          if (dl[d]) { atomicAdd(&acc[d], (unsigned long long)dl[d]); dl[d] = 0; }
-        }
-        __syncwarp();
-      }
+      if (s_rel32)
+        seq_streams<K, WPL, uint32_t>(next, d, rows, reinterpret_cast<const uint32_t *>(base32), dl, acc, lane,
+                                      a.err);
+      else
+        seq_streams<K, WPL, unsigned long long>(next, d, rows, base, dl, acc, lane, a.err);
       __syncthreads();
       for (int i = tid; i <= d; i += NW * 32) {
         const unsigned long long v = acc[i];
@@ -726,12 +785,6 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
       }
     }
     __syncthreads();
-  }
-  if constexpr (MODE == MODE_SEQ) {
-    if (a.cliques) {
-      visited = warp_sum(visited);
-      if (lane == 0 && visited) atomicAdd(a.cliques, visited);
-    }
   }
 }
 

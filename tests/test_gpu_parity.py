@@ -152,6 +152,24 @@ def test_tiers_seq_pass_from_nonzero_r(ctx, name, k):
 
 
 @pytest.mark.parametrize("name,k", TIER_CASES)
+def test_tiers_seq_pass_wide_values(ctx, name, k):
+    """Values whose spread inside a root exceeds 2^31 (the kernel then keeps
+    64-bit values; otherwise it works on 32-bit values relative to the root's
+    minimum) and values near the top of the u64 range."""
+    P = TIERS[name]
+    g = dev_graph(ctx, P)
+    og = O.Graph(P)
+    rng = np.random.default_rng(300 + k)
+    choices = np.array([0, 1, 2, 7, 2**31 - 5, 2**31 + 3, 2**40, 2**62], dtype=np.uint64)
+    r0 = choices[rng.integers(0, len(choices), size=g.n)] + rng.integers(0, 3, size=g.n, dtype=np.uint64)
+    r = K.seq_passes(g, k, 1, r0)
+    assert np.array_equal(r, og.seq_pass(k, r0, mode=O.SEQ_EDGE_STREAMS, threads=THREADS))
+    # near the 32-bit boundary for every root: a spread just under and just over
+    r1 = (np.uint64(2**31 - 2**22) * (np.arange(g.n, dtype=np.uint64) % np.uint64(2))).astype(np.uint64)
+    assert np.array_equal(K.seq_passes(g, k, 1, r1), og.seq_pass(k, r1, mode=O.SEQ_EDGE_STREAMS, threads=THREADS))
+
+
+@pytest.mark.parametrize("name,k", TIER_CASES)
 @pytest.mark.parametrize("waves", [16, 5])
 def test_tiers_seq_waves(ctx, name, k, waves):
     """Wave-ordered passes: each wave's chains start from r as the earlier
