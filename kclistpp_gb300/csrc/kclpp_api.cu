@@ -79,7 +79,7 @@ struct kclpp_graph {
   int device = 0;
   HostDag dag;
   // Schedule knobs (tier bounds, stealing); the autotuner may change them.
-  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1, {0, 0, 0, 0}};
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1, {0, 0, 0, 0}, 256, 512};
   // KCLPP_SEQ_WAVES: one Seq schedule per wave (roots grouped by a fixed hash).
   std::vector<std::vector<TierInfo>> wave_tiers;
   std::vector<uint32_t> wave_base;
@@ -208,6 +208,8 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
   uint32_t mx = 0;
   for (int sch = 0; sch < 2; ++sch) {
     const uint32_t smax = sch == 0 ? g->sp.tier_s_max : g->sp.tier_s_max_seq;
+    const uint32_t split1 = sch == 0 ? g->sp.m_split1 : g->sp.seq_split1;
+    const uint32_t split2 = sch == 0 ? g->sp.m_split2 : g->sp.seq_split2;
     std::vector<uint32_t> tS, tM1, tM2, tM3, tL;
     for (uint32_t s = 0; s < D.n; ++s) {
       const uint32_t d = deg(s);
@@ -215,8 +217,8 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
       if (g->shard_world > 1 && g->owner[s] != g->shard_rank) continue;
       mx = std::max(mx, d);
       if (d <= smax) tS.push_back(s);
-      else if (d <= g->sp.m_split1) tM1.push_back(s);
-      else if (d <= g->sp.m_split2) tM2.push_back(s);
+      else if (d <= split1) tM1.push_back(s);
+      else if (d <= split2) tM2.push_back(s);
       else if (d <= kTierMMax) tM3.push_back(s);
       else tL.push_back(s);
     }
@@ -261,8 +263,8 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
       for (uint32_t s : grp[w]) {
         const uint32_t d = deg(s);
         if (d <= g->sp.tier_s_max_seq) tS.push_back(s);
-        else if (d <= g->sp.m_split1) tM1.push_back(s);
-        else if (d <= g->sp.m_split2) tM2.push_back(s);
+        else if (d <= g->sp.seq_split1) tM1.push_back(s);
+        else if (d <= g->sp.seq_split2) tM2.push_back(s);
         else if (d <= kTierMMax) tM3.push_back(s);
         else tL.push_back(s);
       }
@@ -877,7 +879,8 @@ static kclpp_status check_schedule(const kclpp_schedule *sp) {
   if (sp->seq_waves < 1 || sp->seq_waves > 1024)
     return set_error(KCLPP_ERR_INVALID, "seq_waves must be in [1, 1024]");
   if (sp->tier_s_max > kTierSMax || sp->tier_s_max_seq > kTierSMax || sp->m_split1 < sp->tier_s_max ||
-      sp->m_split1 < sp->tier_s_max_seq || sp->m_split2 < sp->m_split1 || sp->m_split2 > kTierMMax)
+      sp->m_split2 < sp->m_split1 || sp->m_split2 > kTierMMax || sp->seq_split1 < sp->tier_s_max_seq ||
+      sp->seq_split2 < sp->seq_split1 || sp->seq_split2 > kTierMMax)
     return set_error(KCLPP_ERR_INVALID, "schedule bounds out of range (tier S <= %u <= split1 <= split2 <= %u)",
                      kTierSMax, kTierMMax);
   return KCLPP_OK;
@@ -979,8 +982,8 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
         for (uint32_t sm : smax) {
           kclpp_schedule x = base;
           x.tier_s_max_seq = sm;
-          x.m_split1 = splits[sp][0];
-          x.m_split2 = splits[sp][1];
+          x.seq_split1 = splits[sp][0];
+          x.seq_split2 = splits[sp][1];
           x.steal_seq = st == 0;
           cand.push_back(x);
         }
