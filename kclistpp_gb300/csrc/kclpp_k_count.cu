@@ -62,7 +62,7 @@ static cudaError_t noalloc_tier(int tier, dev::PassArgs a, int sms, cudaStream_t
   }
   static LaunchCache lc;
   constexpr int NW = kWarpsM;
-  const size_t sm = layout_m(MODE_COUNT, a.dmax, NW, true).total;
+  const size_t sm = layout_m(MODE_COUNT, K, a.dmax, NW, true).total;
   auto fn = tier_m_kernel<MODE_COUNT, K, 1, true, true>;
   cudaError_t e = prepare(fn, lc, NW * 32, sm, &per_sm);
   if (e != cudaSuccess) return e;

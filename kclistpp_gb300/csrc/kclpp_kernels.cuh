@@ -382,13 +382,56 @@ __device__ __forceinline__ uint64_t cnt_warp(const Bits<WPL> &P, const uint32_t 
   }
 }
 
+// Edges of G_s inside P, each once, as per-lane partial sums (the k = 4 count,
+// (k-2)-cliques = edges): the counting rows are symmetric and each member y
+// counts its neighbours below it (BELOW), the Order rows are oriented upward
+// and y counts its whole row.  P's members are compacted and a lane takes one
+// member at a time, walking only the words its row can occupy -- instead of
+// a warp per member over all W words (cnt_warp), which leaves the lanes past
+// W idle and re-reads the empty half of every row.  scratch: 32 words for P,
+// then the member list (u16).
+template <bool BELOW>
+__device__ __forceinline__ uint32_t edges_in(const Bits<1> &P, const uint32_t *rows, int W, int lane,
+                                             uint32_t *scratch) {
+  uint16_t *members = reinterpret_cast<uint16_t *>(scratch + 32);
+  if (lane < W) scratch[lane] = P.w[0];
+  const uint32_t lt = lanemask_lt();
+  uint32_t total = 0;
+  uint32_t nz = __ballot_sync(KCL_FULL, P.w[0] != 0);
+  while (nz) {
+    const int L = __ffs(nz) - 1;
+    nz &= nz - 1;
+    const uint32_t word = __shfl_sync(KCL_FULL, P.w[0], L);
+    if ((word >> lane) & 1u) members[total + __popc(word & lt)] = (uint16_t)((L << 5) | lane);
+    total += (uint32_t)__popc(word);
+  }
+  __syncwarp();
+  uint32_t c = 0;
+  for (uint32_t i = lane; i < total; i += 32) {
+    const int y = members[i];
+    const uint32_t *ry = rows + (size_t)y * W;
+    if constexpr (BELOW) {
+      const int hi = y >> 5;
+      for (int w = 0; w < hi; ++w) c += __popc(scratch[w] & ry[w]);
+      c += __popc(scratch[hi] & ry[hi] & ((1u << (y & 31)) - 1u));
+    } else {
+      for (int w = y >> 5; w < W; ++w) c += __popc(scratch[w] & ry[w]);
+    }
+  }
+  __syncwarp();  // the next row reuses the scratch
+  return c;
+}
+
 // Shared-memory layout of a tier M / L CTA (dmax = largest out-degree the
 // launch allows, NW warps).  Tier L keeps `rows` in a global slab instead.
 struct LayoutM {
-  size_t list, rows, base, base32, acc, rank, inv, dl, total;
+  size_t list, rows, base, base32, acc, rank, inv, dl, cbuf, total;
 };
+// Per-warp scratch of the k = 4 counting path (edges_in): P's words and its
+// members, compacted.
+__host__ __device__ inline size_t cbuf_words(uint32_t dmax) { return 32 + (dmax + 1) / 2; }
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
-__host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, bool rows_in_smem) {
+__host__ __device__ inline LayoutM layout_m(int mode, int k, uint32_t dmax, int nw, bool rows_in_smem) {
   LayoutM L;
   const size_t W = (dmax + 31) / 32;
   size_t at = 0;
@@ -401,6 +444,8 @@ __host__ __device__ inline LayoutM layout_m(int mode, uint32_t dmax, int nw, boo
   L.rank = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
   L.inv = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
   L.dl = at; if (mode == MODE_SEQ) at = align16(at + (size_t)nw * (dmax + 1) * 4);
+  L.cbuf = at;
+  if (mode != MODE_SEQ && k == 4 && rows_in_smem) at = align16(at + (size_t)nw * cbuf_words(dmax) * 4);
   L.total = at;
   return L;
 }
@@ -591,7 +636,7 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
   const int NW = (int)(blockDim.x >> 5);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int dmax = (int)a.dmax;
-  const LayoutM lay = layout_m(MODE, a.dmax, NW, ROWS_IN_SMEM);
+  const LayoutM lay = layout_m(MODE, K, a.dmax, NW, ROWS_IN_SMEM);
   uint32_t *list = reinterpret_cast<uint32_t *>(smem_raw + lay.list);
   uint32_t *rows = ROWS_IN_SMEM ? reinterpret_cast<uint32_t *>(smem_raw + lay.rows)
                                 : a.slab + (size_t)blockIdx.x * a.slab_words;
@@ -600,6 +645,7 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
   uint16_t *rank = reinterpret_cast<uint16_t *>(smem_raw + lay.rank);
   uint16_t *inv = reinterpret_cast<uint16_t *>(smem_raw + lay.inv);
   uint32_t *dl = reinterpret_cast<uint32_t *>(smem_raw + lay.dl) + (size_t)wid * (dmax + 1);
+  uint32_t *cbuf = reinterpret_cast<uint32_t *>(smem_raw + lay.cbuf) + (size_t)wid * cbuf_words(a.dmax);
 
   __shared__ uint32_t s_idx;
   __shared__ int s_tau;
@@ -756,15 +802,21 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
         p = __shfl_sync(KCL_FULL, p, 0);
         if (p >= d) break;
         const Bits<WPL> P = load_row<WPL>(rows, p, W, lane);
-        uint64_t c = cnt_warp<K - 2, MODE == MODE_COUNT, WPL>(P, rows, W, lane);
-        c = warp_sum(c);
+        uint64_t c = 0;
         uint64_t c_low = 0;
-        if constexpr (MODE == MODE_COUNT) {
-          // s's own share: the (k-1)-cliques of G_s whose largest member is p,
-          // i.e. the (k-2)-cliques among p's neighbours below it.  Summing these
-          // (instead of dividing the row total by k-1) stays exact when several
-          // CTAs split one root.
-          c_low = warp_sum(cnt_warp<K - 2, true, WPL>(band(P, below_mask<WPL>(p, lane)), rows, W, lane));
+        if constexpr (K == 4 && WPL == 1 && ROWS_IN_SMEM) {
+          c = warp_sum((uint64_t)edges_in<MODE == MODE_COUNT>(P, rows, W, lane, cbuf));
+          if constexpr (MODE == MODE_COUNT)
+            c_low = warp_sum((uint64_t)edges_in<true>(band(P, below_mask<WPL>(p, lane)), rows, W, lane, cbuf));
+        } else {
+          c = warp_sum(cnt_warp<K - 2, MODE == MODE_COUNT, WPL>(P, rows, W, lane));
+          if constexpr (MODE == MODE_COUNT) {
+            // s's own share: the (k-1)-cliques of G_s whose largest member is p,
+            // i.e. the (k-2)-cliques among p's neighbours below it.  Summing
+            // these (instead of dividing the row total by k-1) stays exact when
+            // several CTAs split one root.
+            c_low = warp_sum(cnt_warp<K - 2, true, WPL>(band(P, below_mask<WPL>(p, lane)), rows, W, lane));
+          }
         }
         if (lane == 0) {
           if (MODE == MODE_COUNT) {
@@ -832,7 +884,7 @@ static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int
 // that keeps the most warps resident per SM at this out-degree bound (ties:
 // the narrower, i.e. more CTAs).  Seq: 8..24 in steps of 4; the counting
 // kernels: 8..32 in steps of 8.
-template <int MODE, typename Fn>
+template <int MODE, int K, typename Fn>
 static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
   using namespace dev;
   constexpr int lo = 8, hi = warps_m<MODE>(), step = MODE == MODE_SEQ ? 4 : 8;
@@ -844,7 +896,7 @@ static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_i
   int best = 0, best_warps = -1;
   for (int w = lo; w <= hi; w += step) {
     if (req > 0 && w != req) continue;
-    const size_t sm = layout_m(MODE, dmax, w, rows_in_smem).total;
+    const size_t sm = layout_m(MODE, K, dmax, w, rows_in_smem).total;
     if (sm > 227 * 1024) continue;
     int per_sm = 0;
     cudaError_t e = prepare(fn, lc, w * 32, sm, &per_sm);
@@ -900,9 +952,9 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
     static LaunchCache lc;
     auto fn = tier_m_kernel<MODE, K, 1, true>;
     int nw = kWarpsM;
-    cudaError_t e = pick_warps<MODE>(fn, lc, t.dmax, true, t.warps, &nw);
+    cudaError_t e = pick_warps<MODE, K>(fn, lc, t.dmax, true, t.warps, &nw);
     if (e != cudaSuccess) return e;
-    const size_t sm = layout_m(MODE, t.dmax, nw, true).total;
+    const size_t sm = layout_m(MODE, K, t.dmax, nw, true).total;
     e = prepare(fn, lc, nw * 32, sm, &per_sm);
     if (e != cudaSuccess) return e;
     fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), nw * 32, sm, st>>>(a);
@@ -911,9 +963,9 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
   static LaunchCache lc;
   auto fn = tier_m_kernel<MODE, K, 2, false>;
   int nw = kWarpsM;
-  cudaError_t e = pick_warps<MODE>(fn, lc, t.dmax, false, t.warps, &nw);
+  cudaError_t e = pick_warps<MODE, K>(fn, lc, t.dmax, false, t.warps, &nw);
   if (e != cudaSuccess) return e;
-  const size_t sm = layout_m(MODE, t.dmax, nw, false).total;
+  const size_t sm = layout_m(MODE, K, t.dmax, nw, false).total;
   e = prepare(fn, lc, nw * 32, sm, &per_sm);
   if (e != cudaSuccess) return e;
   fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), nw * 32, sm, st>>>(a);
