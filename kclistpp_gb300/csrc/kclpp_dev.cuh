@@ -68,6 +68,15 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(KCL_FULL, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+
 // Ordering key of a vertex for MODE_ORDER: the clique credits its smallest key.
 //  KEY_SIM:   (rho bits, id) -- rho >= 0, so the IEEE bit pattern orders as the
 //             value; ties go to the smaller id (kCDensestCmpSync.c:139-143).

@@ -425,7 +425,7 @@ __device__ __forceinline__ uint32_t edges_in(const Bits<1> &P, const uint32_t *r
 // Shared-memory layout of a tier M / L CTA (dmax = largest out-degree the
 // launch allows, NW warps).  Tier L keeps `rows` in a global slab instead.
 struct LayoutM {
-  size_t list, rows, base, base32, acc, rank, inv, dl, cbuf, total;
+  size_t list, rows, base, acc, rank, inv, dl, cbuf, total;
 };
 // Per-warp scratch of the k = 4 counting path (edges_in): P's words and its
 // members, compacted.
@@ -439,7 +439,6 @@ __host__ __device__ inline LayoutM layout_m(int mode, int k, uint32_t dmax, int 
   L.rows = at;
   if (rows_in_smem) at = align16(at + (mode == MODE_SEQ ? (size_t)tri_off(dmax) : (size_t)dmax * W) * 4);
   L.base = at; if (mode != MODE_COUNT) at = align16(at + (size_t)(dmax + 1) * 8);
-  L.base32 = at; if (mode == MODE_SEQ) at = align16(at + (size_t)(dmax + 1) * 4);
   L.acc = at; if (mode == MODE_SEQ) at = align16(at + (size_t)(dmax + 1) * 8);
   L.rank = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
   L.inv = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
@@ -450,23 +449,42 @@ __host__ __device__ inline LayoutM layout_m(int mode, int k, uint32_t dmax, int 
   return L;
 }
 
-// The Seq chain over V (the last level), one 32-bit word of V at a time: lane
-// b stands for candidate 32 * word + b.  c is the current value of the prefix
-// argmin (kCDensestNoAtom.c:162-171 and 180-186: each clique goes to the
-// candidate w when r[w] < c, strict, else to the prefix argmin, whose value
-// then grows by one).  Inside a word the chain is resolved by a ballot fixed
-// point on 32-bit distances: rel = r[w] - c (-1 when r[w] < c, which always
-// takes the clique), and candidate i falls to the prefix iff rel_i >= the
-// number of earlier candidates of the word that fell to it.  Returns the
-// prefix argmin's new value.
-//
-// T is the value type: unsigned long long (pass-start r as is; distances
-// clamped to 2^31 - 1), or uint32_t when the root's values were stored
-// relative to their minimum and every value the stream can reach stays below
-// 2^31, so that a plain 32-bit difference is the distance.
-//
-// Vertex x's delta dl[x] is only ever read and written by lane x & 31 (here,
-// and for the argmin updates of seq_rec), so the chains need no warp barrier.
+// Current values of a root-edge stream's vertices (pass-start r plus the
+// stream's own increments), in one of two forms:
+//  * Vals32: one u32 per vertex, offset from the smallest pass-start value of
+//    the stream (off) and capped at cap, when every value the stream can reach
+//    stays below 2^31 (see seq_stream);
+//  * Vals64: the pass-start u64 plus a u32 delta per vertex.
+// Vertex x's word is only ever read and written by lane x & 31 (the chain,
+// the argmin write-backs, the stream's setup and close), so the chains need
+// no warp barrier.
+struct Vals32 {
+  using T = uint32_t;
+  uint32_t *cur;
+  __device__ __forceinline__ T get(int v, uint32_t &raw) const { raw = cur[v]; return raw; }
+  __device__ __forceinline__ void bump(int v, uint32_t raw, uint32_t *) const { cur[v] = raw + 1u; }
+  __device__ __forceinline__ void add(int v, T delta, uint32_t *) const { cur[v] += delta; }
+};
+template <bool OVF>
+struct Vals64 {
+  using T = unsigned long long;
+  const unsigned long long *base;
+  uint32_t *dl;
+  __device__ __forceinline__ T get(int v, uint32_t &raw) const { raw = dl[v]; return base[v] + raw; }
+  __device__ __forceinline__ void bump(int v, uint32_t raw, uint32_t *err) const {
+    if (OVF && raw == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
+    dl[v] = raw + 1u;
+  }
+  __device__ __forceinline__ void add(int v, T delta, uint32_t *err) const {
+    const unsigned long long nd = (unsigned long long)dl[v] + delta;
+    if (OVF && nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
+    dl[v] = (uint32_t)nd;
+  }
+};
+
+// Distance from the prefix value c to a candidate's value, as the chain's
+// fixed point uses it: -1 below c, else the difference clamped to 2^31 - 1
+// (a plain 32-bit difference for Vals32, whose values all lie below 2^31).
 template <typename T>
 __device__ __forceinline__ int distance(T av, T c) {
   if constexpr (sizeof(T) == 4) {
@@ -478,9 +496,18 @@ __device__ __forceinline__ int distance(T av, T c) {
   }
 }
 
-template <int WPL, bool OVF, typename T>
-__device__ __forceinline__ T chain_words(const Bits<WPL> &V, T c, const T *base, uint32_t *dl, int lane,
-                                         uint32_t *err) {
+// The Seq chain over V (the last level), one 32-bit word of V at a time: lane
+// b stands for candidate 32 * word + b.  c is the current value of the prefix
+// argmin (kCDensestNoAtom.c:162-171 and 180-186: each clique goes to the
+// candidate w when r[w] < c, strict, else to the prefix argmin, whose value
+// then grows by one).  Inside a word the chain is resolved by a ballot fixed
+// point: candidate i falls to the prefix iff its distance to c is >= the
+// number of earlier candidates of the word that fell to it.  Returns the
+// prefix argmin's new value.
+template <int WPL, typename VA>
+__device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typename VA::T c, const VA &va,
+                                                      int lane, uint32_t *err) {
+  using T = typename VA::T;
   const uint32_t lt = lanemask_lt();
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
@@ -492,62 +519,60 @@ __device__ __forceinline__ T chain_words(const Bits<WPL> &V, T c, const T *base,
       const bool valid = (word >> lane) & 1u;
       const int v = ((L + 32 * q) << 5) | lane;
       int rel = -1;
-      uint32_t dv = 0;
-      if (valid) {
-        dv = dl[v];
-        rel = distance<T>(base[v] + dv, c);
-      }
+      uint32_t raw = 0;
+      if (valid) rel = distance<T>(va.get(v, raw), c);
+      // Fixed point from "every candidate at or above c falls": once the
+      // loads have spread, that guess is already exact and one vote confirms
+      // it; ties (the first pass) take a few more rounds.
       uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
-      for (int r = 0; r < 33; ++r) {
-        const uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
-        if (m2 == m) break;
+      uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+      if (m2 != m) {
         m = m2;
+        for (int r = 0; r < 32; ++r) {
+          m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+          if (m2 == m) break;
+          m = m2;
+        }
       }
-      if (valid && !((m >> lane) & 1u)) {
-        if (OVF && dv == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
-        dl[v] = dv + 1u;
-      }
+      if (valid && !((m >> lane) & 1u)) va.bump(v, raw, err);
       c += (T)__popc(m);
     }
   }
   return c;
 }
 
-// Current value of vertex x (pass-start r plus this stream's delta), read by
-// the lane that owns dl[x] and broadcast.
-template <typename T>
-__device__ __forceinline__ T value_of(int x, const T *base, const uint32_t *dl, int lane) {
-  T v = 0;
-  if ((x & 31) == lane) v = base[x] + dl[x];
+// Current value of vertex x, read by the lane that owns it and broadcast.
+template <typename VA>
+__device__ __forceinline__ typename VA::T value_of(int x, const VA &va, int lane) {
+  typename VA::T v = 0;
+  uint32_t raw;
+  if ((x & 31) == lane) v = va.get(x, raw);
   return __shfl_sync(KCL_FULL, v, x & 31);
 }
 
 // Level L of a root-edge stream over candidates P with prefix argmin g of
 // current value cg (kCDensestNoAtom.c:173-188 for L = 2, 237-259 above).
 // Returns g's new value; the argmin of a deeper prefix, when it is u, is
-// written back to dl[u] by u's lane.
-template <int L, int WPL, bool OVF, typename T>
-__device__ __forceinline__ T seq_rec(const Bits<WPL> &P, T cg, const uint32_t *rows, const T *base, uint32_t *dl,
-                                     int lane, uint32_t *err) {
+// written back by u's lane.
+template <int L, int WPL, typename VA>
+__device__ __forceinline__ typename VA::T seq_rec(const Bits<WPL> &P, typename VA::T cg, const uint32_t *rows,
+                                                  const VA &va, int lane, uint32_t *err) {
+  using T = typename VA::T;
   if constexpr (L == 1) {
-    return chain_words<WPL, OVF, T>(P, cg, base, dl, lane, err);
+    return chain_words<WPL, VA>(P, cg, va, lane, err);
   } else {
     if constexpr (L >= 3) {
       const int pc = warp_sum(popc_lane(P));  // kCDensestNoAtom.c:218
       if (pc < L) return cg;
     }
     for_each_bit<WPL>(P, [&](int u) {
-      const T vu = value_of<T>(u, base, dl, lane);
+      const T vu = value_of<VA>(u, va, lane);
       const bool take = vu < cg;  // strict: ties stay with the earlier argmin
       const Bits<WPL> Q = band(P, load_row<WPL, true>(rows, u, 0, lane));
       const T c0 = take ? vu : cg;
-      const T c1 = seq_rec<L - 1, WPL, OVF, T>(Q, c0, rows, base, dl, lane, err);
+      const T c1 = seq_rec<L - 1, WPL, VA>(Q, c0, rows, va, lane, err);
       if (take) {
-        if (lane == (u & 31)) {
-          const unsigned long long nd = (unsigned long long)dl[u] + (unsigned long long)(c1 - c0);
-          if (OVF && nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
-          dl[u] = (uint32_t)nd;
-        }
+        if (lane == (u & 31)) va.add(u, c1 - c0, err);
       } else {
         cg = c1;
       }
@@ -556,12 +581,36 @@ __device__ __forceinline__ T seq_rec(const Bits<WPL> &P, T cg, const uint32_t *r
   }
 }
 
+// Apply f(i) on the lane owning each member i of C (lane i & 31).
+template <int WPL, typename F>
+__device__ __forceinline__ void for_members(const Bits<WPL> &C, int lane, F &&f) {
+#pragma unroll
+  for (int qq = 0; qq < WPL; ++qq) {
+    uint32_t nz = __ballot_sync(KCL_FULL, C.w[qq] != 0);
+    while (nz) {
+      const int L = __ffs(nz) - 1;
+      nz &= nz - 1;
+      const uint32_t word = __shfl_sync(KCL_FULL, C.w[qq], L);
+      if ((word >> lane) & 1u) f(((L + 32 * qq) << 5) | lane);
+    }
+  }
+}
+
 // Every root-edge stream of the current root, the warp taking streams from
 // the root's shared counter (largest candidate sets first); increments go to
 // the CTA's acc[] (kCDensestNoAtom.c:270-295 per root edge).
-template <int K, int WPL, typename T>
-__device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_t *rows, const T *base,
-                                            uint32_t *dl, unsigned long long *acc, int lane, uint32_t *err) {
+//
+// A stream's values fit the 32-bit form when, with off = the smallest
+// pass-start value among {s, t} and C and cap = (the edge argmin's value
+// - off) + the most increments one vertex can take in the stream + 64, cap
+// stays below 2^31: values above cap are stored as cap, which changes no
+// comparison -- the prefix value never exceeds cap - 64, so such a candidate
+// falls to the prefix whatever came before it (its distance is >= 64 > 31),
+// and it never becomes the prefix argmin.
+template <int K, int WPL>
+__device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_t *rows,
+                                            const unsigned long long *base, uint32_t *cur,
+                                            unsigned long long *acc, int lane, uint32_t *err) {
   for (;;) {
     int q = 0;
     if (lane == 0) q = (int)atomicAdd(next, 1u);
@@ -571,34 +620,50 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
     const Bits<WPL> C = load_row<WPL, true>(rows, j, 0, lane);
     if (!any_bits<WPL>(C)) continue;
     const int g0 = base[j] < base[d] ? j : d;  // kCDensestNoAtom.c:287
-    const T c0 = base[g0];
-    const T c1 = seq_rec<K - 2, WPL, (K >= 6), T>(C, c0, rows, base, dl, lane, err);
-    // Close the stream: its increments fell on C (each member's delta held
-    // by its own lane) and on the edge's argmin g0 (held in c1).
-#pragma unroll
-    for (int qq = 0; qq < WPL; ++qq) {
-      uint32_t nz = __ballot_sync(KCL_FULL, C.w[qq] != 0);
-      while (nz) {
-        const int L = __ffs(nz) - 1;
-        nz &= nz - 1;
-        const uint32_t word = __shfl_sync(KCL_FULL, C.w[qq], L);
-        if ((word >> lane) & 1u) {
-          const int i = ((L + 32 * qq) << 5) | lane;
-          const uint32_t v = dl[i];
-          if (v) { atomicAdd(&acc[i], (unsigned long long)v); dl[i] = 0; }
-        }
-      }
+    bool r32 = false;
+    unsigned long long off = 0, cap = 0;
+    if constexpr (K <= 5) {
+      unsigned long long lo = base[g0];
+      int nc = 0;
+      for_members<WPL>(C, lane, [&](int i) {
+        const unsigned long long b = base[i];
+        lo = b < lo ? b : lo;
+        ++nc;
+      });
+      lo = warp_min_u64(lo);
+      nc = warp_sum(nc);
+      unsigned long long bound = 1;  // C(nc, K - 2) >= the increments of one vertex
+      for (int i = 0; i < K - 2; ++i) bound = bound * (unsigned long long)(nc - i) / (unsigned long long)(i + 1);
+      off = lo;
+      cap = (base[g0] - lo) + bound + 64;
+      r32 = cap < 0x7fffffffull;
     }
-    if (lane == 0 && c1 != c0) atomicAdd(&acc[g0], (unsigned long long)(c1 - c0));
+    if (r32) {
+      for_members<WPL>(C, lane, [&](int i) {
+        const unsigned long long rel = base[i] - off;
+        cur[i] = (uint32_t)(rel < cap ? rel : cap);
+      });
+      const Vals32 va{cur};
+      const uint32_t c0 = (uint32_t)(base[g0] - off);
+      const uint32_t c1 = seq_rec<K - 2, WPL, Vals32>(C, c0, rows, va, lane, err);
+      for_members<WPL>(C, lane, [&](int i) {
+        const unsigned long long rel = base[i] - off;
+        const uint32_t delta = cur[i] - (uint32_t)(rel < cap ? rel : cap);
+        if (delta) atomicAdd(&acc[i], (unsigned long long)delta);
+      });
+      if (lane == 0 && c1 != c0) atomicAdd(&acc[g0], (unsigned long long)(c1 - c0));
+    } else {
+      for_members<WPL>(C, lane, [&](int i) { cur[i] = 0; });
+      const Vals64<(K >= 6)> va{base, cur};
+      const unsigned long long c0 = base[g0];
+      const unsigned long long c1 = seq_rec<K - 2, WPL, Vals64<(K >= 6)>>(C, c0, rows, va, lane, err);
+      for_members<WPL>(C, lane, [&](int i) {
+        const uint32_t delta = cur[i];
+        if (delta) atomicAdd(&acc[i], (unsigned long long)delta);
+      });
+      if (lane == 0 && c1 != c0) atomicAdd(&acc[g0], c1 - c0);
+    }
   }
-}
-
-// Largest increment one vertex can take within a stream of a root with out-
-// degree d: the (k-2)-subsets of a candidate set of at most d - 1 members.
-__device__ __forceinline__ unsigned long long stream_bound(int K, int d) {
-  unsigned long long b = 1;
-  for (int i = 0; i < K - 2; ++i) b = b * (unsigned long long)(d - 1 - i) / (unsigned long long)(i + 1);
-  return b;
 }
 
 // Work stealing: once the root list is exhausted, an idle CTA joins a root
@@ -650,9 +715,6 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
   __shared__ uint32_t s_idx;
   __shared__ int s_tau;
   __shared__ unsigned long long s_sum;
-  __shared__ unsigned long long s_min, s_max;
-  __shared__ bool s_rel32;
-  uint32_t *base32 = reinterpret_cast<uint32_t *>(smem_raw + lay.base32);
 
   if constexpr (MODE == MODE_SEQ) {
     for (int i = tid; i <= dmax; i += NW * 32) acc[i] = 0;
@@ -704,36 +766,9 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
     }
     if constexpr (MODE == MODE_SEQ) {
       for (int i = tid; i < d; i += NW * 32) base[i] = a.r_in[a.cols[o + i]];
-      if (tid == 0) {
-        base[d] = a.r_in[s];
-        s_min = ~0ull;
-        s_max = 0;
-      }
+      if (tid == 0) base[d] = a.r_in[s];
     }
     __syncthreads();
-    if constexpr (MODE == MODE_SEQ) {
-      // 32-bit values relative to the root's minimum when every value a stream
-      // can reach stays below 2^31 (k <= 5 only: deeper streams can exceed it).
-      if constexpr (K <= 5) {
-        unsigned long long lo = ~0ull, hi = 0;
-        for (int i = tid; i <= d; i += NW * 32) {
-          const unsigned long long v = base[i];
-          lo = v < lo ? v : lo;
-          hi = v > hi ? v : hi;
-        }
-        atomicMin(&s_min, lo);
-        atomicMax(&s_max, hi);
-        __syncthreads();
-        const unsigned long long mn = s_min;
-        const bool r32 = s_max - mn + stream_bound(K, d) < 0x7fffffffull;
-        if (r32)
-          for (int i = tid; i <= d; i += NW * 32) base32[i] = (uint32_t)(base[i] - mn);
-        if (tid == 0) s_rel32 = r32;
-      } else {
-        if (tid == 0) s_rel32 = false;
-      }
-      __syncthreads();
-    }
     if constexpr (MODE == MODE_ORDER) {
       const unsigned long long ks = base[d];
       int t = 0;
@@ -780,11 +815,7 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
       __syncthreads();
     }
     if constexpr (MODE == MODE_SEQ) {
-      if (s_rel32)
-        seq_streams<K, WPL, uint32_t>(next, d, rows, reinterpret_cast<const uint32_t *>(base32), dl, acc, lane,
-                                      a.err);
-      else
-        seq_streams<K, WPL, unsigned long long>(next, d, rows, base, dl, acc, lane, a.err);
+      seq_streams<K, WPL>(next, d, rows, base, dl, acc, lane, a.err);
       __syncthreads();
       for (int i = tid; i <= d; i += NW * 32) {
         const unsigned long long v = acc[i];
