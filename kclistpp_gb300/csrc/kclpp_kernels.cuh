@@ -504,14 +504,37 @@ __device__ __forceinline__ int distance(T av, T c) {
 // point: candidate i falls to the prefix iff its distance to c is >= the
 // number of earlier candidates of the word that fell to it.  Returns the
 // prefix argmin's new value.
-template <int WPL, typename VA>
+//
+// lo (Vals32, one word per lane): the smallest value the stream started with
+// among C's members in that lane's word of the bitmap.  Values only grow, so
+// a word of V whose candidates all start at or above c + (candidates before
+// them) falls to the prefix whole; the leading run of such words is settled
+// by one scan and skipped.
+template <int WPL, typename VA, bool SKIP>
 __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typename VA::T c, const VA &va,
-                                                      int lane, uint32_t *err) {
+                                                      uint32_t lo, int lane, uint32_t *err) {
   using T = typename VA::T;
   const uint32_t lt = lanemask_lt();
+  uint32_t skip_mask = 0;
+  if constexpr (SKIP && WPL == 1) {
+    const uint32_t pop = (uint32_t)__popc(V.w[0]);
+    uint32_t incl = pop;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(KCL_FULL, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const bool ok = pop == 0 || lo >= (uint32_t)c + (incl - 1);
+    const uint32_t bad = __ballot_sync(KCL_FULL, !ok);
+    const int fb = bad ? __ffs(bad) - 1 : 32;
+    if (fb > 0) {
+      c += (T)__shfl_sync(KCL_FULL, incl, fb - 1);
+      skip_mask = fb == 32 ? 0xffffffffu : (1u << fb) - 1u;
+    }
+  }
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
-    uint32_t nz = __ballot_sync(KCL_FULL, V.w[q] != 0);
+    uint32_t nz = __ballot_sync(KCL_FULL, V.w[q] != 0) & (q == 0 ? ~skip_mask : 0xffffffffu);
     while (nz) {
       const int L = __ffs(nz) - 1;
       nz &= nz - 1;
@@ -554,12 +577,12 @@ __device__ __forceinline__ typename VA::T value_of(int x, const VA &va, int lane
 // current value cg (kCDensestNoAtom.c:173-188 for L = 2, 237-259 above).
 // Returns g's new value; the argmin of a deeper prefix, when it is u, is
 // written back by u's lane.
-template <int L, int WPL, typename VA>
+template <int L, int WPL, typename VA, bool SKIP>
 __device__ __forceinline__ typename VA::T seq_rec(const Bits<WPL> &P, typename VA::T cg, const uint32_t *rows,
-                                                  const VA &va, int lane, uint32_t *err) {
+                                                  const VA &va, uint32_t lo, int lane, uint32_t *err) {
   using T = typename VA::T;
   if constexpr (L == 1) {
-    return chain_words<WPL, VA>(P, cg, va, lane, err);
+    return chain_words<WPL, VA, SKIP>(P, cg, va, lo, lane, err);
   } else {
     if constexpr (L >= 3) {
       const int pc = warp_sum(popc_lane(P));  // kCDensestNoAtom.c:218
@@ -570,7 +593,7 @@ __device__ __forceinline__ typename VA::T seq_rec(const Bits<WPL> &P, typename V
       const bool take = vu < cg;  // strict: ties stay with the earlier argmin
       const Bits<WPL> Q = band(P, load_row<WPL, true>(rows, u, 0, lane));
       const T c0 = take ? vu : cg;
-      const T c1 = seq_rec<L - 1, WPL, VA>(Q, c0, rows, va, lane, err);
+      const T c1 = seq_rec<L - 1, WPL, VA, SKIP>(Q, c0, rows, va, lo, lane, err);
       if (take) {
         if (lane == (u & 31)) va.add(u, c1 - c0, err);
       } else {
@@ -639,13 +662,29 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
       r32 = cap < 0x7fffffffull;
     }
     if (r32) {
-      for_members<WPL>(C, lane, [&](int i) {
-        const unsigned long long rel = base[i] - off;
-        cur[i] = (uint32_t)(rel < cap ? rel : cap);
-      });
+      // Stored values, and per word of C the smallest of them (lane = word).
+      uint32_t lo = 0xffffffffu;
+#pragma unroll
+      for (int qq = 0; qq < WPL; ++qq) {
+        uint32_t nz = __ballot_sync(KCL_FULL, C.w[qq] != 0);
+        while (nz) {
+          const int L = __ffs(nz) - 1;
+          nz &= nz - 1;
+          const uint32_t word = __shfl_sync(KCL_FULL, C.w[qq], L);
+          uint32_t val = 0xffffffffu;
+          if ((word >> lane) & 1u) {
+            const int i = ((L + 32 * qq) << 5) | lane;
+            const unsigned long long rel = base[i] - off;
+            val = (uint32_t)(rel < cap ? rel : cap);
+            cur[i] = val;
+          }
+          val = __reduce_min_sync(KCL_FULL, val);
+          if (qq == 0 && lane == L) lo = val;
+        }
+      }
       const Vals32 va{cur};
       const uint32_t c0 = (uint32_t)(base[g0] - off);
-      const uint32_t c1 = seq_rec<K - 2, WPL, Vals32>(C, c0, rows, va, lane, err);
+      const uint32_t c1 = seq_rec<K - 2, WPL, Vals32, (WPL == 1)>(C, c0, rows, va, lo, lane, err);
       for_members<WPL>(C, lane, [&](int i) {
         const unsigned long long rel = base[i] - off;
         const uint32_t delta = cur[i] - (uint32_t)(rel < cap ? rel : cap);
@@ -656,7 +695,7 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
       for_members<WPL>(C, lane, [&](int i) { cur[i] = 0; });
       const Vals64<(K >= 6)> va{base, cur};
       const unsigned long long c0 = base[g0];
-      const unsigned long long c1 = seq_rec<K - 2, WPL, Vals64<(K >= 6)>>(C, c0, rows, va, lane, err);
+      const unsigned long long c1 = seq_rec<K - 2, WPL, Vals64<(K >= 6)>, false>(C, c0, rows, va, 0u, lane, err);
       for_members<WPL>(C, lane, [&](int i) {
         const uint32_t delta = cur[i];
         if (delta) atomicAdd(&acc[i], (unsigned long long)delta);
