@@ -517,6 +517,7 @@ __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typena
   const uint32_t lt = lanemask_lt();
   uint32_t skip_mask = 0;
   if constexpr (SKIP && WPL == 1) {
+    if (!__any_sync(KCL_FULL, V.w[0] != 0)) return c;
     const uint32_t pop = (uint32_t)__popc(V.w[0]);
     uint32_t incl = pop;
 #pragma unroll
