@@ -298,14 +298,17 @@ def batch_workload(K, ctx, a) -> dict:
         d = float(rng.uniform(8, 64))
         els.append(K.erdos_renyi(n, d, seed=1000 + i) if i % 2 else K.chung_lu(n, d, 2.5, seed=1000 + i))
     gen_s = time.perf_counter() - t0
+    print(f"batch: generated {len(els)} graphs in {gen_s:.1f} s", file=sys.stderr, flush=True)
     t0 = time.perf_counter()
     b = K.Batch(ctx, els)
     build_s = time.perf_counter() - t0
+    print(f"batch: union of {b.n} vertices, {b.m} edges built in {build_s:.1f} s", file=sys.stderr, flush=True)
     ks = [3, 4, 5, 6, 7]
     T = a.batch_passes
     t0 = time.perf_counter()
     out = b.run(K.KERNEL_SEQ, ks, T)  # captures the CUDA graph
     first_s = time.perf_counter() - t0
+    print(f"batch: first run (capture + replay) {first_s:.1f} s", file=sys.stderr, flush=True)
     # every pass gives each k-clique one unit: the r vectors sum to T x the count
     visits = int(sum(int(out[i].sum()) for i in range(len(ks))))
     times = []

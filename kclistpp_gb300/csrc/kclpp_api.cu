@@ -69,6 +69,11 @@ static cudaEvent_t take_event(kclpp_ctx *c) {
   return e;
 }
 
+// Scheduler words of a pass: root counters of up to 5 launch groups, then one
+// stealing registry (kActiveSlots words) per group.
+constexpr size_t kWorkActive = 32;
+constexpr size_t kWorkWords = kWorkActive + 5 * (size_t)kActiveSlots;
+
 struct TierInfo {
   int tier;
   int bucket;  // 0..3: the M1, M2, M3 and L root groups (kclpp_schedule.seq_warps); -1: tier S
@@ -99,7 +104,8 @@ struct kclpp_graph {
   unsigned long long *d_a = nullptr, *d_b = nullptr;
   double *d_rho = nullptr;
   uint32_t *d_level = nullptr;
-  uint32_t *d_work = nullptr;   // [0,16): root counters per tier; [16,32): steal cursors
+  uint32_t *d_work = nullptr;   // [0,16): root counters per tier; from kWorkActive: the
+                                // stealing registries, kActiveSlots words per tier
   uint32_t *d_task = nullptr;   // per-root sub-task counters (tiers M, L)
   uint32_t num_roots = 0;
   uint32_t task_cap = 0;
@@ -292,7 +298,7 @@ static kclpp_status build_schedule(kclpp_ctx *c, kclpp_graph *g) {
   KCL_TRY(dalloc(&g->d_roots, all.size()));
   if (!all.empty())
     KCL_CUDA(cudaMemcpyAsync(g->d_roots, all.data(), all.size() * 4, cudaMemcpyHostToDevice, c->stream));
-  KCL_TRY(dalloc(&g->d_work, 32));
+  KCL_TRY(dalloc(&g->d_work, kWorkWords));
   if (g->num_roots > g->task_cap) {  // the counters must cover every root of the schedule
     cudaFree(g->d_task);
     g->d_task = nullptr;
@@ -346,7 +352,7 @@ static void free_graph_dev(kclpp_graph *g) {
 // (the batch's k values) each need their own counters.
 struct Exec {
   cudaStream_t st;
-  uint32_t *work;  // 32 words
+  uint32_t *work;  // kWorkWords words
   uint32_t *task;  // one per root
 };
 
@@ -359,7 +365,8 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
   const uint32_t base = wv ? g->wave_base[wave] : g->sched_base[sch];
   if (tiers.empty()) return KCLPP_OK;
   const Exec E = ex ? *ex : Exec{c->stream, g->d_work, g->d_task};
-  KCL_CUDA(cudaMemsetAsync(E.work, 0, 32 * sizeof(uint32_t), E.st));
+  KCL_CUDA(cudaMemsetAsync(E.work, 0, kWorkActive * sizeof(uint32_t), E.st));
+  KCL_CUDA(cudaMemsetAsync(E.work + kWorkActive, 0xff, (kWorkWords - kWorkActive) * sizeof(uint32_t), E.st));
   KCL_CUDA(cudaMemsetAsync(E.task, 0, (size_t)g->num_roots * sizeof(uint32_t), E.st));
   a.off = g->d_off;
   a.cols = g->d_cols;
@@ -388,7 +395,7 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
     // Work stealing pays off for the Seq chains (long, uneven root edges); the
     // counting kernels finish their roots quickly and by default do not steal.
     const bool steal = mode == dev::MODE_SEQ ? g->sp.steal_seq != 0 : g->sp.steal_count != 0;
-    tl.steal_cursor = steal ? E.work + 16 + i : nullptr;
+    tl.active = steal ? E.work + kWorkActive + i * kActiveSlots : nullptr;
     tl.num_sms = c->num_sms;
     tl.max_grid = t.tier == 2 ? g->slab_ctas : 0;
     tl.warps = t.bucket < 0 ? 0 : (int)(mode == dev::MODE_SEQ ? g->sp.seq_warps[t.bucket] : g->sp.count_warps[t.bucket]);
@@ -1229,7 +1236,7 @@ kclpp_status kclpp_batch_run(kclpp_ctx *c, kclpp_batch *b, int kernel, const int
       x.k = ks[i];
       KCL_CUDA(cudaStreamCreateWithFlags(&x.st, cudaStreamNonBlocking));
       KCL_CUDA(cudaEventCreateWithFlags(&x.join, cudaEventDisableTiming));
-      KCL_TRY(dalloc(&x.work, 32));
+      KCL_TRY(dalloc(&x.work, kWorkWords));
       KCL_TRY(dalloc(&x.task, std::max<uint32_t>(g->num_roots, 1)));
       KCL_TRY(dalloc(&x.buf[0], n));
       if (kernel == KCLPP_KERNEL_SEQ) KCL_TRY(dalloc(&x.buf[1], n));

@@ -42,7 +42,7 @@ struct PassArgs {
   uint32_t dmax;                  // largest out-degree among them
   uint32_t *work;                 // root counter (zeroed before launch)
   uint32_t *task_next;            // tiers M, L: per-root sub-task counters (zeroed)
-  uint32_t *steal_cursor;         // tiers M, L: first root that may have sub-tasks left
+  uint32_t *active;               // tiers M, L: one slot per CTA, the root it holds (nullptr: no stealing)
   uint32_t *err;                  // status word
   int key_kind;                   // MODE_ORDER
   const double *rho;              // KEY_SIM
@@ -107,7 +107,7 @@ struct TierLaunch {
   uint32_t dmax;
   uint32_t *work;
   uint32_t *task_next;
-  uint32_t *steal_cursor;
+  uint32_t *active;  // kActiveSlots slots (nullptr: no stealing)
   int num_sms;
   int max_grid;      // upper bound on CTAs (tier L: CTAs the row slab holds)
   int warps;         // tiers M / L: warps per CTA (0 = the most resident warps)
@@ -133,5 +133,7 @@ constexpr uint32_t kTierSMax = 64;
 constexpr uint32_t kTierSMaxSeq = 16;
 constexpr uint32_t kTierMMax = 1024;
 constexpr uint32_t kTierLMax = 2048;
+// Slots of a stealing launch's root registry (its grid is capped to this).
+constexpr uint32_t kActiveSlots = 2048;
 
 }  // namespace kclpp

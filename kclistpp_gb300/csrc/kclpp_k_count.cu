@@ -141,7 +141,7 @@ extern "C" kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, ui
     if (e == cudaSuccess) {
       dev::PassArgs s = a;
       s.work = scr + 1;
-      s.steal_cursor = scr + 2;
+      s.active = nullptr;  // no stealing: the registry would need one slot per CTA
       s.dmax = kTierMMax;
       s.deg_lo = dev::kSMaxD + 1;
       s.deg_hi = UINT32_MAX;

@@ -708,23 +708,30 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
 
 // Work stealing: once the root list is exhausted, an idle CTA joins a root
 // whose sub-tasks (root edges or rows) are not all taken, rebuilds that root's
-// G_s and takes sub-tasks from the same global counter.  The cursor skips
-// roots known to be exhausted, so the scans cost O(roots) in total.
+// G_s and takes sub-tasks from the same global counter.  Every CTA publishes
+// the root it holds in its slot of a.active, so a thief looks at the roots in
+// progress only (one slot per CTA, scanned by one warp) and joins the one with
+// the most sub-tasks left.  Returns UINT32_MAX when none has kMinSteal left.
 constexpr uint32_t kMinSteal = 2;
 template <bool IDENT>
-__device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need) {
-  uint32_t c = *(volatile uint32_t *)a.steal_cursor;
-  while (c < a.num_roots) {
-    const uint32_t s = IDENT ? c : a.roots[c];
+__device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need, int lane) {
+  uint32_t best = 0, best_idx = UINT32_MAX;  // best = sub-tasks left (0: none)
+  for (uint32_t b = lane; b < gridDim.x; b += 32) {
+    const uint32_t idx = *(volatile uint32_t *)(a.active + b);
+    if (idx >= a.num_roots) continue;
+    const uint32_t s = IDENT ? idx : a.roots[idx];
     const uint32_t d = (uint32_t)(a.off[s + 1] - a.off[s]);
-    const uint32_t taken = *(volatile uint32_t *)(a.task_next + c);
+    const uint32_t taken = *(volatile uint32_t *)(a.task_next + idx);
     const bool in_window = !IDENT || (d >= a.deg_lo && d <= a.deg_hi && d <= a.dmax);
-    if (in_window && (int)d >= need && taken + kMinSteal <= d) return c;
-    atomicMax(a.steal_cursor, c + 1);
-    const uint32_t c2 = *(volatile uint32_t *)a.steal_cursor;
-    c = c2 > c + 1 ? c2 : c + 1;
+    if (in_window && (int)d >= need && taken + kMinSteal <= d && d - taken > best) {
+      best = d - taken;
+      best_idx = idx;
+    }
   }
-  return UINT32_MAX;
+  const uint32_t top = __reduce_max_sync(KCL_FULL, best);
+  if (top == 0) return UINT32_MAX;
+  const uint32_t who = __ballot_sync(KCL_FULL, best == top);
+  return __shfl_sync(KCL_FULL, best_idx, __ffs(who) - 1);
 }
 
 // Register budget of a tier M / L kernel, as CTAs of the widest launch that
@@ -760,19 +767,23 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
     for (int i = tid; i <= dmax; i += NW * 32) acc[i] = 0;
     for (int i = lane; i <= dmax; i += 32) dl[i] = 0;
   }
-  bool stealing = false;  // read by thread 0 only
+  bool stealing = false;  // warp 0's view (uniform across its lanes)
   __syncthreads();
   for (;;) {
-    if (tid == 0) {
+    if (wid == 0) {
       uint32_t idx = UINT32_MAX;
       if (!stealing) {
-        idx = atomicAdd(a.work, 1u);
+        if (lane == 0) idx = atomicAdd(a.work, 1u);
+        idx = __shfl_sync(KCL_FULL, idx, 0);
         if (idx >= a.num_roots) stealing = true;
       }
-      if (stealing) idx = a.steal_cursor ? find_victim<IDENT>(a, K - 1) : UINT32_MAX;
-      s_idx = idx;
-      s_tau = 0;
-      s_sum = 0;
+      if (stealing) idx = a.active ? find_victim<IDENT>(a, K - 1, lane) : UINT32_MAX;
+      if (lane == 0) {
+        s_idx = idx;
+        s_tau = 0;
+        s_sum = 0;
+        if (a.active && idx != UINT32_MAX) a.active[blockIdx.x] = idx;  // visible to thieves
+      }
     }
     __syncthreads();
     const uint32_t idx = s_idx;
@@ -907,6 +918,7 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
         if constexpr (IDENT && MODE == MODE_COUNT) atomicAdd(a.total, s_sum);
       }
     }
+    if (tid == 0 && a.active) a.active[blockIdx.x] = UINT32_MAX;
     __syncthreads();
   }
 }
@@ -996,6 +1008,7 @@ static int persistent_grid(int per_sm, const TierLaunch &t, int roots_per_cta, b
     if (need < g) g = need;
   }
   if (t.max_grid > 0 && g > t.max_grid) g = t.max_grid;
+  if (steals && g > (long long)kActiveSlots) g = kActiveSlots;  // one registry slot per CTA
   return (int)(g < 1 ? 1 : g);
 }
 
@@ -1007,7 +1020,7 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
   a.dmax = t.dmax;
   a.work = t.work;
   a.task_next = t.task_next;
-  a.steal_cursor = t.steal_cursor;
+  a.active = t.active;
   if (t.num_roots == 0) return cudaSuccess;
   int per_sm = 1;
   if (t.tier == 0) {
@@ -1028,7 +1041,7 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
     const size_t sm = layout_m(MODE, K, t.dmax, nw, true).total;
     e = prepare(fn, lc, nw * 32, sm, &per_sm);
     if (e != cudaSuccess) return e;
-    fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), nw * 32, sm, st>>>(a);
+    fn<<<persistent_grid(per_sm, t, 1, t.active != nullptr), nw * 32, sm, st>>>(a);
     return cudaGetLastError();
   }
   static LaunchCache lc;
@@ -1039,7 +1052,7 @@ cudaError_t launch_tier(const TierLaunch &t, dev::PassArgs a, cudaStream_t st) {
   const size_t sm = layout_m(MODE, K, t.dmax, nw, false).total;
   e = prepare(fn, lc, nw * 32, sm, &per_sm);
   if (e != cudaSuccess) return e;
-  fn<<<persistent_grid(per_sm, t, 1, t.steal_cursor != nullptr), nw * 32, sm, st>>>(a);
+  fn<<<persistent_grid(per_sm, t, 1, t.active != nullptr), nw * 32, sm, st>>>(a);
   return cudaGetLastError();
 }
 
