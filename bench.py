@@ -348,7 +348,8 @@ def main() -> None:
     ap.add_argument("--batch-nmax", type=float, default=1e5)
     ap.add_argument("--batch-passes", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=-1,
+                    help="steps of the host-buffer run (default: --steps, replaying the timed passes)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-convergence", action="store_true",
@@ -477,6 +478,10 @@ def main() -> None:
         step()
     ctx.synchronize()
     torch.cuda.synchronize()
+    # the state the timed passes start from (the host-buffer run replays them)
+    r_start = r_dev.cpu().numpy().view(np.uint64).copy()
+    rho_start = rho_dev.cpu().numpy().copy()
+    t_start = t_sim[0]
     if dist:
         dist.barrier()
     clocks = ClockSampler(local)
@@ -558,7 +563,8 @@ def main() -> None:
 
     # ---- end to end through the C ABI with host buffers -------------------------------
     e2e = None
-    if a.e2e_steps > 0 and world == 1:
+    e2e_steps = a.steps if a.e2e_steps < 0 else a.e2e_steps
+    if e2e_steps > 0 and world == 1:
         off_h = torch.empty(len(off), dtype=torch.int64, pin_memory=True).numpy().view(np.uint64)
         off_h[:] = off
         cols_h = torch.empty(len(cols), dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
@@ -584,10 +590,15 @@ def main() -> None:
                                                      rho_h.ctypes.data_as(C.POINTER(C.c_double))))
             g2.close()
 
-        e2e_step(1)  # warm
+        r_h[:] = r_start
+        rho_h[:] = rho_start
+        e2e_step(t_start)  # warm
+        # the same passes as the timed region: from the same r / rho and pass index
+        r_h[:] = r_start
+        rho_h[:] = rho_start
         e2e_t = []
-        tt = 2
-        for _ in range(a.e2e_steps):
+        tt = t_start
+        for _ in range(e2e_steps):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             e2e_step(tt)
@@ -599,8 +610,8 @@ def main() -> None:
         graph_bytes = 8 * (n + 1) + 4 * g.m + 4 * g.m + 8 * roots * (1 + len(sched))
         h2d = graph_bytes + 8 * n * len(modes)
         d2h = (8 * n + 4) * len(modes)
-        e2e = {"value": per_step / statistics.median(e2e_t), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "steps": a.e2e_steps,
+        e2e = {"value": per_step / (sum(e2e_t) / len(e2e_t)), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                "api": "kclpp_graph_from_csr + kclpp_graph_set_schedule + kclpp_seq_passes / kclpp_sim_passes "
                       "(host CSR + host r / rho, pinned)"}
 
