@@ -148,10 +148,11 @@ typedef struct {
   uint32_t seq_warps[4];    /* Seq kernel, warps per CTA of the M1 (<= seq_split1), M2 (<= split2), */
                             /* M3 (<= 1024) and L root groups: 8, 12, 16, 20 or 24; 0 = the width  */
                             /* that keeps the most warps resident per SM                           */
-  int concurrent_tiers;     /* launch a pass's root groups on forked streams (default 1)          */
+  int concurrent_tiers;     /* Seq kernel: launch a pass's root groups on forked streams (def. 1)  */
   uint32_t count_warps[4];  /* the counting / Sim kernels' widths of the same four groups:         */
                             /* 8, 16, 24 or 32; 0 = the most resident warps per SM                 */
   uint32_t seq_split1, seq_split2; /* the Seq kernel's tier M groups (as m_split1, m_split2)        */
+  int concurrent_count;     /* the counting / Sim kernels' root groups on forked streams (def. 1)  */
 } kclpp_schedule;
 kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp);
 kclpp_status kclpp_graph_set_schedule(kclpp_ctx *ctx, kclpp_graph *g, const kclpp_schedule *sp);

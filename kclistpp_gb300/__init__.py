@@ -79,7 +79,7 @@ class Schedule(C.Structure):
                 ("m_split2", C.c_uint32), ("steal_seq", C.c_int), ("steal_count", C.c_int),
                 ("seq_waves", C.c_uint32), ("seq_warps", C.c_uint32 * 4),
                 ("concurrent_tiers", C.c_int), ("count_warps", C.c_uint32 * 4),
-                ("seq_split1", C.c_uint32), ("seq_split2", C.c_uint32)]
+                ("seq_split1", C.c_uint32), ("seq_split2", C.c_uint32), ("concurrent_count", C.c_int)]
 
     def __init__(self, **kw):
         arr = {f: t for f, t in self._fields_ if issubclass(t, C.Array)}

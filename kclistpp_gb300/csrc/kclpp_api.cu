@@ -84,7 +84,7 @@ struct kclpp_graph {
   int device = 0;
   HostDag dag;
   // Schedule knobs (tier bounds, stealing); the autotuner may change them.
-  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1, {0, 0, 0, 0}, 256, 512};
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1, {0, 0, 0, 0}, 256, 512, 1};
   // KCLPP_SEQ_WAVES: one Seq schedule per wave (roots grouped by a fixed hash).
   std::vector<std::vector<TierInfo>> wave_tiers;
   std::vector<uint32_t> wave_base;
@@ -377,7 +377,9 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
   // and add into the output), so they may run side by side: the later groups
   // fill the SMs that the first one's tail leaves idle.
   const int nside =
-      (!ex && g->sp.concurrent_tiers && tiers.size() > 1) ? (int)std::min<size_t>(tiers.size() - 1, 4) : 0;
+      (!ex && (mode == dev::MODE_SEQ ? g->sp.concurrent_tiers : g->sp.concurrent_count) && tiers.size() > 1)
+          ? (int)std::min<size_t>(tiers.size() - 1, 4)
+          : 0;
   if (nside) {
     KCL_CUDA(cudaEventRecord(c->fork_ev, E.st));
     for (int j = 0; j < nside; ++j) KCL_CUDA(cudaStreamWaitEvent(c->side[j], c->fork_ev, 0));
@@ -1037,7 +1039,7 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
     for (int wi = 0; wi < nwid; ++wi) {
       const uint32_t w = widths[wi];
       kclpp_schedule x = best_sp;
-      x.concurrent_tiers = 0;  // each group's own launch time
+      (sq ? x.concurrent_tiers : x.concurrent_count) = 0;  // each group's own launch time
       for (int b = 0; b < 4; ++b) (sq ? x.seq_warps : x.count_warps)[b] = w;
       KCL_TRY(kclpp_graph_set_schedule(c, g, &x));
       std::vector<float> ms;
@@ -1062,7 +1064,8 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
   {
     // Root groups side by side or one after another.
     kclpp_schedule x = best_sp;
-    x.concurrent_tiers = !best_sp.concurrent_tiers;
+    if (mode == dev::MODE_SEQ) x.concurrent_tiers = !best_sp.concurrent_tiers;
+    else x.concurrent_count = !best_sp.concurrent_count;
     KCL_TRY(kclpp_graph_set_schedule(c, g, &x));
     float ms = 0.f;
     KCL_TRY(time_pass(c, g, k, mode, &ms));
