@@ -254,7 +254,7 @@ kclpp_status kclpp_sim_passes_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const 
                                   const uint32_t *cols, int k, uint32_t t_first, uint32_t passes,
                                   double *rho_inout);
 
-/* ---- sharded passes (no reference counterpart) ---------------
+/* ---- sharded passes (roots split over ranks; no reference counterpart) -----
  * A pass splits over devices by root: every rank builds the same graph,
  * restricts it to its share of roots with kclpp_graph_shard, computes its
  * part with the *_delta / *_counts entry points below, and the ranks sum the

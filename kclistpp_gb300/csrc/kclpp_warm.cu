@@ -12,7 +12,7 @@
 //              backward with a warp per vertex (each lane owns two hidden
 //              units and their gradients; one global fp32 atomic per parameter
 //              per warp), then an Adam step
-// The plain zero-start run stays the fallback and the judge: the warm start
+// The plain zero-start run stays the fallback and the yardstick: the warm start
 // changes only where the passes start, and its upper bound is computed from
 // the increments the passes add (a feasible load), never from the prediction.
 #include <cuda_bf16.h>
