@@ -78,3 +78,39 @@ def test_batch_of_config4_shape(ctx):
         g = K.build_graph(ctx, els[gi])
         for ki, k in enumerate(ks):
             assert np.array_equal(out[ki, b.slice(gi)], K.seq_passes(g, k, 4))
+
+
+def _knob_graph():
+    # many small roots (stealing among them) next to a few dense ones (all
+    # tier M groups in use)
+    els = [K.chung_lu(4000, 20.0, 2.3, seed=51), K.erdos_renyi(3000, 30.0, seed=52),
+           K.planted(3000, 6.0, 2.2, 1, 1400, 1400, 0.5, seed=53)]
+    pairs, base = [], 0
+    for el in els:
+        p = el.pairs().astype(np.int64)
+        pairs.append(p + base)
+        base += el.n
+    return K.EdgeList.from_pairs(np.concatenate(pairs))
+
+
+def test_schedule_knobs_change_no_result(ctx):
+    """Tier bounds, group splits, CTA widths, work stealing and concurrent
+    groups decide only where and when work runs: every combination gives the
+    default schedule's r / counts bit for bit."""
+    g = K.build_graph(ctx, _knob_graph())
+    rng = np.random.default_rng(9)
+    r0 = rng.integers(0, 5, size=g.n, dtype=np.uint64) * np.uint64(7)
+    rho0 = rng.integers(0, 3, size=g.n).astype(np.float64) * 0.5
+    want = {k: (K.seq_passes(g, k, 2, r0), K.sim_counts(g, k, rho0)) for k in (4, 5)}
+    base = K.get_schedule(g)
+    combos = [dict(steal_seq=s, steal_count=s, concurrent_tiers=c, concurrent_count=c, seq_warps=[w] * 4,
+                   count_warps=[cw] * 4, tier_s_max=ts, tier_s_max_seq=tq, seq_split1=a, seq_split2=b,
+                   m_split1=a, m_split2=b)
+              for s, c, w, cw, ts, tq, a, b in [(0, 0, 8, 8, 64, 8, 128, 256), (1, 1, 24, 32, 32, 32, 256, 512),
+                                                (1, 0, 16, 16, 64, 16, 384, 768), (0, 1, 20, 24, 16, 64, 512, 1024)]]
+    for cb in combos:
+        sp = K.Schedule(**{**base.as_dict(), **cb})
+        K.set_schedule(g, sp)
+        for k, (r_want, c_want) in want.items():
+            assert np.array_equal(K.seq_passes(g, k, 2, r0), r_want), (cb, k)
+            assert np.array_equal(K.sim_counts(g, k, rho0), c_want), (cb, k)
