@@ -516,8 +516,14 @@ __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typena
   using T = typename VA::T;
   const uint32_t lt = lanemask_lt();
   uint32_t skip_mask = 0;
+  uint32_t nz0 = 0;  // SKIP: the nonzero words of V, computed once
   if constexpr (SKIP && WPL == 1) {
-    if (!__any_sync(KCL_FULL, V.w[0] != 0)) return c;
+    nz0 = __ballot_sync(KCL_FULL, V.w[0] != 0);
+    if (!nz0) return c;
+  }
+  // The scan pays off from two words on; a single word goes straight to its
+  // own fixed point.
+  if (SKIP && WPL == 1 && (nz0 & (nz0 - 1))) {
     const uint32_t pop = (uint32_t)__popc(V.w[0]);
     uint32_t incl = pop;
 #pragma unroll
@@ -535,7 +541,7 @@ __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typena
   }
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
-    uint32_t nz = __ballot_sync(KCL_FULL, V.w[q] != 0) & (q == 0 ? ~skip_mask : 0xffffffffu);
+    uint32_t nz = (SKIP && WPL == 1) ? (nz0 & ~skip_mask) : __ballot_sync(KCL_FULL, V.w[q] != 0);
     while (nz) {
       const int L = __ffs(nz) - 1;
       nz &= nz - 1;
