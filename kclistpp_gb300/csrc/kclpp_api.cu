@@ -416,9 +416,16 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
       cudaEventRecord(pt.b, ls);
       c->pending.push_back(pt);
     }
-    if (e != cudaSuccess)
+    if (e != cudaSuccess) {
+      // Join what the side streams already hold before reporting, so that the
+      // caller's stream orders after every launch of this pass.
+      for (int j = 0; j < nside; ++j) {
+        cudaEventRecord(c->join_ev[j], c->side[j]);
+        cudaStreamWaitEvent(E.st, c->join_ev[j], 0);
+      }
       return set_error(KCLPP_ERR_CUDA, "kernel launch (mode %d, tier %d, k %d): %s", mode, t.tier, k,
                        cudaGetErrorString(e));
+    }
     c->launches++;
   }
   for (int j = 0; j < nside; ++j) {
