@@ -125,8 +125,8 @@ def dag_stats(off: np.ndarray, cols: np.ndarray, k: int, s_max: int = 64, split1
         t["dmax"] = max(t["dmax"], int(deg[s]))
         if active[s]:
             t["impl_bytes"] += int(impl_root[s])
-            if edge_root is not None:
-                t["bytes"] += int(edge_root[s])
+        if edge_root is not None:
+            t["bytes"] += int(edge_root[s])
     return {"tiers": tiers, "survey_bytes_per_pass": survey, "n": n, "m": int(len(cols))}
 
 

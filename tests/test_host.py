@@ -117,3 +117,32 @@ def test_oracle_pins_config1_hash():
     p = G.pairs("config1_chung_lu_1e4")
     assert len(p) == 96552
     assert hashlib.sha256(p.tobytes()).hexdigest() == G.index()["config1_chung_lu_1e4"]["sha256"]
+
+
+def test_bench_byte_model_matches_brute_force():
+    """bench.py's roofline bytes: the per-root-edge gathers of the reference's
+    MakeSubgraph, 8 + 4(d+s + d+t) + 4 sum_{x in C(s,t)} d+x + 8(|C(s,t)| + 2)
+    per root edge plus 8(n+1) + 16n per pass, checked against a direct count."""
+    import importlib.util
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "bench.py")
+    spec = importlib.util.spec_from_file_location("kclpp_bench", path)
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    og = O.Graph(K.planted(1500, 6.0, 2.2, 1, 80, 80, 0.5, seed=61).pairs())
+    off, cols = og.csr()
+    off = off.astype(np.int64)
+    cols = cols.astype(np.int64)
+    n = len(off) - 1
+    deg = np.diff(off)
+    want = 8 * (n + 1) + 16 * n
+    for s in range(n):
+        Ns = set(cols[off[s]:off[s + 1]].tolist())
+        for t in cols[off[s]:off[s + 1]]:
+            C = Ns & set(cols[off[t]:off[t + 1]].tolist())
+            want += 8 + 4 * (deg[s] + deg[t]) + 4 * sum(deg[x] for x in C) + 8 * (len(C) + 2)
+    st = bench.dag_stats(off.astype(np.uint64), cols.astype(np.uint32), 4)
+    assert st["survey_bytes_per_pass"] == want
+    # the per-tier figures partition the per-root-edge part
+    assert sum(v["bytes"] for v in st["tiers"].values()) == want - 8 * (n + 1) - 16 * n
