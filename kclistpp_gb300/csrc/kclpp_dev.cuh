@@ -124,8 +124,10 @@ constexpr int kWarpsS = 4;
 constexpr int kWarpsM = 8;
 constexpr int kWarpsMMax = 32;
 constexpr int kWarpsMSeqMax = 24;
-template <int MODE>
-constexpr int warps_m() { return MODE == dev::MODE_SEQ ? kWarpsMSeqMax : kWarpsMMax; }
+// Widest CTA of a tier M / L launch: the counting kernels at k = 5 stop at 24
+// warps so that two CTAs fit the register file at their 42-register budget.
+template <int MODE, int K>
+constexpr int warps_m() { return MODE == dev::MODE_SEQ ? kWarpsMSeqMax : (K == 5 ? 24 : kWarpsMMax); }
 // Tier bounds on a root's out-degree.  The Seq kernel keeps only the smallest
 // roots on tier S (a lane runs a whole root-edge stream there, which is slow
 // on dense roots); the counting kernels use tier S up to 64.

@@ -422,6 +422,53 @@ __device__ __forceinline__ uint32_t edges_in(const Bits<1> &P, const uint32_t *r
   return c;
 }
 
+// Triangles of G_s inside P, each once, as per-lane partial sums (the k = 5
+// count): a lane per member y of P walks the members z of P ∩ row(y) (below y
+// with BELOW) and adds |P ∩ row(y) ∩ row(z)| over the words those rows can
+// occupy.  scratch as in edges_in.
+template <bool BELOW>
+__device__ __forceinline__ uint32_t triangles_in(const Bits<1> &P, const uint32_t *rows, int W, int lane,
+                                                 uint32_t *scratch) {
+  uint16_t *members = reinterpret_cast<uint16_t *>(scratch + 32);
+  if (lane < W) scratch[lane] = P.w[0];
+  const uint32_t lt = lanemask_lt();
+  uint32_t total = 0;
+  uint32_t nz = __ballot_sync(KCL_FULL, P.w[0] != 0);
+  while (nz) {
+    const int L = __ffs(nz) - 1;
+    nz &= nz - 1;
+    const uint32_t word = __shfl_sync(KCL_FULL, P.w[0], L);
+    if ((word >> lane) & 1u) members[total + __popc(word & lt)] = (uint16_t)((L << 5) | lane);
+    total += (uint32_t)__popc(word);
+  }
+  __syncwarp();
+  uint32_t c = 0;
+  for (uint32_t i = lane; i < total; i += 32) {
+    const int y = members[i];
+    const uint32_t *ry = rows + (size_t)y * W;
+    const int lo_w = BELOW ? 0 : (y >> 5), hi_w = BELOW ? (y >> 5) : W - 1;
+    for (int w = lo_w; w <= hi_w; ++w) {
+      uint32_t q = scratch[w] & ry[w];
+      if (BELOW && w == (y >> 5)) q &= (1u << (y & 31)) - 1u;
+      while (q) {
+        const int b = __ffs(q) - 1;
+        q &= q - 1;
+        const int z = (w << 5) | b;
+        const uint32_t *rz = rows + (size_t)z * W;
+        if constexpr (BELOW) {
+          const int zh = z >> 5;
+          for (int w2 = 0; w2 < zh; ++w2) c += __popc(scratch[w2] & ry[w2] & rz[w2]);
+          c += __popc(scratch[zh] & ry[zh] & rz[zh] & ((1u << (z & 31)) - 1u));
+        } else {
+          for (int w2 = z >> 5; w2 < W; ++w2) c += __popc(scratch[w2] & ry[w2] & rz[w2]);
+        }
+      }
+    }
+  }
+  __syncwarp();  // the next row reuses the scratch
+  return c;
+}
+
 // Shared-memory layout of a tier M / L CTA (dmax = largest out-degree the
 // launch allows, NW warps).  Tier L keeps `rows` in a global slab instead.
 struct LayoutM {
@@ -444,7 +491,7 @@ __host__ __device__ inline LayoutM layout_m(int mode, int k, uint32_t dmax, int 
   L.inv = at; if (mode == MODE_ORDER) at = align16(at + (size_t)dmax * 2);
   L.dl = at; if (mode == MODE_SEQ) at = align16(at + (size_t)nw * (dmax + 1) * 4);
   L.cbuf = at;
-  if (mode != MODE_SEQ && k == 4 && rows_in_smem) at = align16(at + (size_t)nw * cbuf_words(dmax) * 4);
+  if (mode != MODE_SEQ && (k == 4 || k == 5) && rows_in_smem) at = align16(at + (size_t)nw * cbuf_words(dmax) * 4);
   L.total = at;
   return L;
 }
@@ -742,14 +789,14 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need, int
 
 // Register budget of a tier M / L kernel, as CTAs of the widest launch that
 // must fit one SM: two for the shallow recursions (the Seq kernel then keeps
-// <= 42 registers a thread at k = 3, 4, the counting kernels <= 32 at k <= 5,
-// so that two wide CTAs are resident), one for the deeper ones, which would
+// <= 42 registers a thread at k = 3, 4; the counting kernels <= 32 at k <= 4
+// and <= 42 at k = 5 with 24-warp CTAs), one for the deeper ones, which would
 // otherwise spill.
 template <int MODE, int K>
 constexpr int min_ctas_m() { return K <= (MODE == MODE_SEQ ? 4 : 5) ? 2 : 1; }
 
 template <int MODE, int K, int WPL, bool ROWS_IN_SMEM, bool IDENT = false>
-__global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) tier_m_kernel(PassArgs a) {
+__global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()) tier_m_kernel(PassArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int NW = (int)(blockDim.x >> 5);
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -896,6 +943,10 @@ __global__ void __launch_bounds__(warps_m<MODE>() * 32, min_ctas_m<MODE, K>()) t
           c = warp_sum((uint64_t)edges_in<MODE == MODE_COUNT>(P, rows, W, lane, cbuf));
           if constexpr (MODE == MODE_COUNT)
             c_low = warp_sum((uint64_t)edges_in<true>(band(P, below_mask<WPL>(p, lane)), rows, W, lane, cbuf));
+        } else if constexpr (K == 5 && WPL == 1 && ROWS_IN_SMEM) {
+          c = warp_sum((uint64_t)triangles_in<MODE == MODE_COUNT>(P, rows, W, lane, cbuf));
+          if constexpr (MODE == MODE_COUNT)
+            c_low = warp_sum((uint64_t)triangles_in<true>(band(P, below_mask<WPL>(p, lane)), rows, W, lane, cbuf));
         } else {
           c = warp_sum(cnt_warp<K - 2, MODE == MODE_COUNT, WPL>(P, rows, W, lane));
           if constexpr (MODE == MODE_COUNT) {
@@ -976,7 +1027,7 @@ static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int
 template <int MODE, int K, typename Fn>
 static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
   using namespace dev;
-  constexpr int lo = 8, hi = warps_m<MODE>(), step = MODE == MODE_SEQ ? 4 : 8;
+  constexpr int lo = 8, hi = warps_m<MODE, K>(), step = MODE == MODE_SEQ ? 4 : 8;
   {
     std::lock_guard<std::mutex> g(lc.mu);
     for (int i = 0; i < lc.nnw; ++i)
@@ -992,7 +1043,7 @@ static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_i
     if (e != cudaSuccess) return e;
     if (per_sm * w > best_warps) { best_warps = per_sm * w; best = w; }
   }
-  if (best == 0) best = 8;
+  if (best == 0) best = req > hi ? hi : lo;  // a width this launch cannot take: the nearest one
   std::lock_guard<std::mutex> g(lc.mu);
   if (lc.nnw < 32) {
     lc.nw_dmax[lc.nnw] = dmax;
