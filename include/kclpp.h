@@ -144,7 +144,7 @@ typedef struct {
                                /* (split2, 1024]                                                  */
   int steal_seq;            /* work stealing in the Seq kernel                                    */
   int steal_count;          /* work stealing in the counting kernels                              */
-  uint32_t seq_waves;       /* waves of KCLPP_SEQ_WAVES, 1..1024 (default 16)                     */
+  uint32_t seq_waves;       /* waves of KCLPP_SEQ_WAVES, 1..1024 (default 4)                      */
   uint32_t seq_warps[4];    /* Seq kernel, warps per CTA of the M1 (<= seq_split1), M2 (<= split2), */
                             /* M3 (<= 1024) and L root groups: 8, 12, 16, 20 or 24; 0 = the width  */
                             /* that keeps the most warps resident per SM                           */
@@ -220,7 +220,7 @@ kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, uint64_t m, c
 #define KCLPP_SEQ_EDGE_STREAMS 1
 /* WAVES: the root vertices are split into waves by a fixed hash of their id,
  * wave w = (uint32_t)(s * 2654435761) % W with W = the graph's
- * kclpp_schedule.seq_waves (default 16); the waves run one after another and
+ * kclpp_schedule.seq_waves (default 4); the waves run one after another and
  * every root edge of a wave runs its chain from r as the earlier waves left
  * it.  A block Gauss-Seidel ordering: the pass's load is balanced across
  * waves, so the upper bound converges in several times fewer passes than

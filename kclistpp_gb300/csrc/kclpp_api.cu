@@ -84,7 +84,7 @@ struct kclpp_graph {
   int device = 0;
   HostDag dag;
   // Schedule knobs (tier bounds, stealing); the autotuner may change them.
-  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 16, {0, 0, 0, 0}, 1, {0, 0, 0, 0}, 256, 512, 1};
+  kclpp_schedule sp = {kTierSMax, kTierSMaxSeq, 256, 512, 1, 0, 4, {0, 0, 0, 0}, 1, {0, 0, 0, 0}, 256, 512, 1};
   // KCLPP_SEQ_WAVES: one Seq schedule per wave (roots grouped by a fixed hash).
   std::vector<std::vector<TierInfo>> wave_tiers;
   std::vector<uint32_t> wave_base;
