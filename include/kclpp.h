@@ -131,12 +131,16 @@ void kclpp_graph_free(kclpp_graph *g);
 kclpp_status kclpp_count_edges(kclpp_ctx *ctx, const kclpp_graph *g, uint32_t num_nodes,
                                const uint32_t *nodes, uint32_t *m_out);
 
-/* Schedule knobs of a device graph (no reference counterpart).  Roots are
- * split into tiers by out-degree: tier S (a warp per root, out-degree <= 64),
- * tier M (a CTA per root, rows in shared memory, out-degree <= 1024, launched
- * in three groups bounded by m_split1 and m_split2 so that smaller roots get a
- * smaller shared-memory footprint and more CTAs per SM), tier L (beyond).
- * Work stealing lets CTAs without a root of their own join unfinished roots. */
+/* Schedule knobs of a device graph (no reference counterpart; none changes a
+ * result).  Roots are split into tiers by out-degree: tier S (a warp per
+ * root, out-degree <= tier_s_max / tier_s_max_seq), tier M (a CTA per root,
+ * rows in shared memory, out-degree <= 1024, launched in three groups bounded
+ * by the two splits of each kernel so that smaller roots get a smaller
+ * shared-memory footprint and more CTAs per SM), tier L (beyond, up to 2048).
+ * Work stealing lets CTAs without a root of their own join the roots other
+ * CTAs are working on.  Defaults: tier_s_max 64, tier_s_max_seq 16, splits
+ * 256 / 512, Seq stealing on, counting stealing off, 4 waves, widths 0 (auto),
+ * concurrent groups on. */
 typedef struct {
   uint32_t tier_s_max;      /* counting kernels (k-clique degrees, Sim, PAVA): tier S bound, <= 64 */
   uint32_t tier_s_max_seq;  /* Seq kernel: tier S bound, <= 64                                    */
@@ -157,8 +161,12 @@ typedef struct {
 kclpp_status kclpp_graph_get_schedule(const kclpp_graph *g, kclpp_schedule *sp);
 kclpp_status kclpp_graph_set_schedule(kclpp_ctx *ctx, kclpp_graph *g, const kclpp_schedule *sp);
 /* Autotuner: times one pass of `kernel` (KCLPP_KERNEL_SEQ or KCLPP_KERNEL_ORDER)
- * at clique size k under each candidate schedule, keeps the fastest on g and
- * reports it.  r / rho start from zero; results are unaffected by the choice. */
+ * at clique size k under each candidate schedule (that kernel's tier bound,
+ * splits and stealing; then its CTA width per group, timed per launch; then
+ * its concurrent groups on / off), keeps the fastest on g and reports it.
+ * Seq is timed on the pass after one pass from zero, the counting kernels from
+ * zero; only the chosen kernel's fields change, so tuning both kernels of a
+ * step on one graph keeps each one's choice. */
 typedef struct {
   kclpp_schedule best;
   double best_ms;           /* one pass under the chosen schedule   */
