@@ -262,6 +262,25 @@ kclpp_status kclpp_sim_passes_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const 
                                   const uint32_t *cols, int k, uint32_t t_first, uint32_t passes,
                                   double *rho_inout);
 
+/* ---- checkpoints (no reference counterpart: its dump of r is commented out,
+ * kCDensestNoAtom.c:398-401).  Host only: a run's vector -- Seq r (u64) or
+ * Sim rho (f64, by bit pattern) -- with the passes done, k and a hash of its
+ * input, so that it resumes where it stopped (for Sim, t_first = passes + 1).
+ * A loaded file is checked (magic, size, checksum): a truncated or altered
+ * checkpoint returns KCLPP_ERR_IO. */
+typedef struct {
+  int kind;             /* KCLPP_KERNEL_SEQ (r) or KCLPP_KERNEL_ORDER (Sim rho) */
+  int k;
+  uint32_t passes;      /* passes done                                        */
+  uint32_t n;           /* vector length                                      */
+  uint64_t graph_hash;  /* kclpp_edge_list_hash of the input, or 0            */
+} kclpp_state_info;
+kclpp_status kclpp_save_state(const char *path, const kclpp_state_info *info, const void *vec);
+/* info receives the header; vec (nullable: header only) holds cap entries. */
+kclpp_status kclpp_load_state(const char *path, kclpp_state_info *info, void *vec, uint32_t cap);
+/* FNV-1a of an edge list's n and pairs (as read or generated). */
+kclpp_status kclpp_edge_list_hash(const kclpp_edge_list *el, uint64_t *hash);
+
 /* ---- sharded passes (roots split over ranks; no reference counterpart) -----
  * A pass splits over devices by root: every rank builds the same graph,
  * restricts it to its share of roots with kclpp_graph_shard, computes its

@@ -65,6 +65,11 @@ class TrimInfo(C.Structure):
                 ("ntrim", C.c_uint32), ("mtrim", C.c_uint64), ("ncktrim", C.c_uint64)]
 
 
+class StateInfo(C.Structure):
+    _fields_ = [("kind", C.c_int), ("k", C.c_int), ("passes", C.c_uint32), ("n", C.c_uint32),
+                ("graph_hash", C.c_uint64)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("mode", C.c_int), ("tier", C.c_int), ("dmax", C.c_uint32), ("launches", C.c_uint32),
                 ("ms", C.c_double)]
@@ -132,6 +137,9 @@ _SIGS = {
     "kclpp_edge_list_info": (C.c_int, [_P, _u32p, _u64p]),
     "kclpp_edge_list_copy": (C.c_int, [_P, _u32p]),
     "kclpp_write_edge_list": (C.c_int, [_P, C.c_char_p]),
+    "kclpp_save_state": (C.c_int, [C.c_char_p, _P, _P]),
+    "kclpp_load_state": (C.c_int, [C.c_char_p, _P, _P, C.c_uint32]),
+    "kclpp_edge_list_hash": (C.c_int, [_P, _u64p]),
     "kclpp_edge_list_free": (None, [_P]),
     "kclpp_generate": (C.c_int, [C.POINTER(GenParams), C.POINTER(_P)]),
     "kclpp_core_order": (C.c_int, [_P, _u32p]),
@@ -295,6 +303,12 @@ class EdgeList:
 
     def write(self, path: str) -> None:
         _check(_lib.kclpp_write_edge_list(self._h, os.fsencode(path)))
+
+    def hash(self) -> int:
+        """FNV-1a of n and the pairs: the graph_hash of a checkpoint."""
+        h = C.c_uint64()
+        _check(_lib.kclpp_edge_list_hash(self._h, C.byref(h)))
+        return h.value
 
     def close(self):
         if getattr(self, "_h", None):
@@ -646,3 +660,21 @@ def trim(ctx: Context, el: EdgeList, k: int, mode: int = TRIM_EXACT) -> TrimResu
         return TrimResult(info, mp, nck, order, core, EdgeList(eh))
     finally:
         _lib.kclpp_trim_free(h)
+
+
+def save_state(path: str, kernel: int, k: int, passes: int, vec: np.ndarray, graph_hash: int = 0) -> None:
+    """Checkpoint of a run: Seq r (uint64, kernel=KERNEL_SEQ) or Sim rho
+    (float64, kernel=KERNEL_ORDER) after `passes` passes."""
+    dt = np.uint64 if kernel == KERNEL_SEQ else np.float64
+    v = np.ascontiguousarray(vec, dtype=dt)
+    info = StateInfo(kernel, k, passes, len(v), graph_hash)
+    _check(_lib.kclpp_save_state(os.fsencode(path), C.byref(info), v.ctypes.data_as(_P)))
+
+
+def load_state(path: str) -> tuple[StateInfo, np.ndarray]:
+    """(header, vector) of a checkpoint; a truncated or altered file raises."""
+    info = StateInfo()
+    _check(_lib.kclpp_load_state(os.fsencode(path), C.byref(info), None, 0))
+    v = np.empty(info.n, dtype=np.uint64 if info.kind == KERNEL_SEQ else np.float64)
+    _check(_lib.kclpp_load_state(os.fsencode(path), C.byref(info), v.ctypes.data_as(_P), info.n))
+    return info, v

@@ -1,0 +1,117 @@
+// kclpp_state.cpp -- checkpoints of a run: the r (Seq) or rho (Sim) vector with
+// the passes done, k and a hash of the DAG, so that a run resumes where it
+// stopped (the reference only has a commented-out dump of r,
+// kCDensestNoAtom.c:398-401).  Host only.
+//
+// File layout (little-endian): "KCLPPST1", u32 kind, u32 k, u32 passes, u32 n,
+// u64 graph hash, n x 8 bytes of the vector, u64 checksum (FNV-1a of every
+// byte before it).
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "kclpp_internal.h"
+
+using namespace kclpp;
+
+namespace {
+
+constexpr char kMagic[8] = {'K', 'C', 'L', 'P', 'P', 'S', 'T', '1'};
+constexpr size_t kHeader = 8 + 4 * 4 + 8;
+
+uint64_t fnv1a(const unsigned char *p, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+  for (size_t i = 0; i < n; ++i) {
+    h ^= p[i];
+    h *= 0x100000001b3ull;
+  }
+  return h;
+}
+
+void put32(unsigned char *p, uint32_t v) {
+  for (int i = 0; i < 4; ++i) p[i] = (unsigned char)(v >> (8 * i));
+}
+void put64(unsigned char *p, uint64_t v) {
+  for (int i = 0; i < 8; ++i) p[i] = (unsigned char)(v >> (8 * i));
+}
+uint32_t get32(const unsigned char *p) {
+  uint32_t v = 0;
+  for (int i = 0; i < 4; ++i) v |= (uint32_t)p[i] << (8 * i);
+  return v;
+}
+uint64_t get64(const unsigned char *p) {
+  uint64_t v = 0;
+  for (int i = 0; i < 8; ++i) v |= (uint64_t)p[i] << (8 * i);
+  return v;
+}
+
+}  // namespace
+
+extern "C" {
+
+kclpp_status kclpp_save_state(const char *path, const kclpp_state_info *info, const void *vec) {
+  if (!path || !info || (!vec && info->n)) return set_error(KCLPP_ERR_INVALID, "kclpp_save_state: null argument");
+  if (info->kind != KCLPP_KERNEL_SEQ && info->kind != KCLPP_KERNEL_ORDER)
+    return set_error(KCLPP_ERR_INVALID, "kclpp_save_state: kind must be KCLPP_KERNEL_SEQ or KCLPP_KERNEL_ORDER");
+  std::vector<unsigned char> buf(kHeader + (size_t)info->n * 8 + 8);
+  memcpy(buf.data(), kMagic, 8);
+  put32(&buf[8], (uint32_t)info->kind);
+  put32(&buf[12], (uint32_t)info->k);
+  put32(&buf[16], info->passes);
+  put32(&buf[20], info->n);
+  put64(&buf[24], info->graph_hash);
+  const unsigned char *src = static_cast<const unsigned char *>(vec);
+  for (uint32_t i = 0; i < info->n; ++i) {
+    uint64_t v;
+    memcpy(&v, src + (size_t)i * 8, 8);  // u64 or the f64 bit pattern
+    put64(&buf[kHeader + (size_t)i * 8], v);
+  }
+  put64(&buf[buf.size() - 8], fnv1a(buf.data(), buf.size() - 8));
+  FILE *f = fopen(path, "wb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s for writing", path);
+  const size_t w = fwrite(buf.data(), 1, buf.size(), f);
+  const int rc = fclose(f);
+  if (w != buf.size() || rc != 0) return set_error(KCLPP_ERR_IO, "write failed: %s", path);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_load_state(const char *path, kclpp_state_info *info, void *vec, uint32_t cap) {
+  if (!path || !info) return set_error(KCLPP_ERR_INVALID, "kclpp_load_state: null argument");
+  FILE *f = fopen(path, "rb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s", path);
+  std::vector<unsigned char> buf;
+  unsigned char chunk[1 << 16];
+  size_t got;
+  while ((got = fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  fclose(f);
+  if (buf.size() < kHeader + 8 || memcmp(buf.data(), kMagic, 8) != 0)
+    return set_error(KCLPP_ERR_IO, "%s is not a kclpp checkpoint", path);
+  const uint32_t n = get32(&buf[20]);
+  if (buf.size() != kHeader + (size_t)n * 8 + 8) return set_error(KCLPP_ERR_IO, "%s: truncated checkpoint", path);
+  if (get64(&buf[buf.size() - 8]) != fnv1a(buf.data(), buf.size() - 8))
+    return set_error(KCLPP_ERR_IO, "%s: checksum mismatch", path);
+  info->kind = (int)get32(&buf[8]);
+  info->k = (int)get32(&buf[12]);
+  info->passes = get32(&buf[16]);
+  info->n = n;
+  info->graph_hash = get64(&buf[24]);
+  if (vec) {
+    if (cap < n) return set_error(KCLPP_ERR_INVALID, "kclpp_load_state: the vector holds %u entries, %u needed", cap, n);
+    unsigned char *dst = static_cast<unsigned char *>(vec);
+    for (uint32_t i = 0; i < n; ++i) {
+      const uint64_t v = get64(&buf[kHeader + (size_t)i * 8]);
+      memcpy(dst + (size_t)i * 8, &v, 8);
+    }
+  }
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_edge_list_hash(const kclpp_edge_list *el, uint64_t *hash) {
+  if (!el || !hash) return set_error(KCLPP_ERR_INVALID, "kclpp_edge_list_hash: null argument");
+  std::vector<unsigned char> b(8 + el->pairs.size() * 4);
+  put64(b.data(), el->n);
+  for (size_t i = 0; i < el->pairs.size(); ++i) put32(&b[8 + 4 * i], el->pairs[i]);
+  *hash = fnv1a(b.data(), b.size());
+  return KCLPP_OK;
+}
+
+}  // extern "C"

@@ -146,3 +146,30 @@ def test_bench_byte_model_matches_brute_force():
     assert st["survey_bytes_per_pass"] == want
     # the per-tier figures partition the per-root-edge part
     assert sum(v["bytes"] for v in st["tiers"].values()) == want - 8 * (n + 1) - 16 * n
+
+
+def test_checkpoint_roundtrip_and_damage(tmp_path):
+    """kclpp_save_state / kclpp_load_state: the vector, pass count, k and input
+    hash come back bit for bit; a truncated, altered or foreign file is
+    reported (KCLPP_ERR_IO), never loaded."""
+    el = K.chung_lu(500, 6.0, 2.5, seed=71)
+    h = el.hash()
+    assert h == K.chung_lu(500, 6.0, 2.5, seed=71).hash() and h != K.chung_lu(500, 6.0, 2.5, seed=72).hash()
+    rng = np.random.default_rng(3)
+    r = rng.integers(0, 2**63, size=el.n, dtype=np.uint64)
+    rho = rng.random(el.n) * 1e6
+    for kern, vec in ((K.KERNEL_SEQ, r), (K.KERNEL_ORDER, rho)):
+        path = str(tmp_path / f"state{kern}.bin")
+        K.save_state(path, kern, 5, 37, vec, h)
+        info, back = K.load_state(path)
+        assert (info.kind, info.k, info.passes, info.n, info.graph_hash) == (kern, 5, 37, el.n, h)
+        assert back.dtype == vec.dtype and np.array_equal(back.view(np.uint64), vec.view(np.uint64))
+    raw = open(path, "rb").read()
+    for bad in (raw[:-3], raw[:40], raw[:16] + bytes([raw[16] ^ 1]) + raw[17:], b"NOTKCLPP" + raw[8:]):
+        p = str(tmp_path / "bad.bin")
+        open(p, "wb").write(bad)
+        with pytest.raises(K.KclppError) as e:
+            K.load_state(p)
+        assert e.value.status == K.ERR_IO
+    with pytest.raises(K.KclppError):
+        K.load_state(str(tmp_path / "missing.bin"))
