@@ -80,6 +80,10 @@ kclpp_status kclpp_profile_read(kclpp_ctx *ctx, kclpp_kernel_time *out, int cap,
 typedef struct kclpp_edge_list kclpp_edge_list;
 /* ReadEdgeList, Graph.c:34-53: "u v" per line, n = max id + 1. */
 kclpp_status kclpp_read_edge_list(const char *path, kclpp_edge_list **out);
+/* The same with `threads` host threads (0: one below 8 MB, else up to 16):
+ * identical results for any count (the numbers are split at whitespace and
+ * the first stop ends the file, as in the one-thread scan). */
+kclpp_status kclpp_read_edge_list_mt(const char *path, int threads, kclpp_edge_list **out);
 /* pairs = s0 t0 s1 t1 ... (2*e entries); n = max id + 1 as in ReadEdgeList. */
 kclpp_status kclpp_edge_list_create(const uint32_t *pairs, uint64_t e, kclpp_edge_list **out);
 kclpp_status kclpp_edge_list_info(const kclpp_edge_list *el, uint32_t *n, uint64_t *e);

@@ -133,6 +133,7 @@ _SIGS = {
     "kclpp_profile_enable": (C.c_int, [_P, C.c_int]),
     "kclpp_profile_read": (C.c_int, [_P, C.POINTER(KernelTime), C.c_int, C.POINTER(C.c_int)]),
     "kclpp_read_edge_list": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
+    "kclpp_read_edge_list_mt": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
     "kclpp_edge_list_create": (C.c_int, [_u32p, C.c_uint64, C.POINTER(_P)]),
     "kclpp_edge_list_info": (C.c_int, [_P, _u32p, _u64p]),
     "kclpp_edge_list_copy": (C.c_int, [_P, _u32p]),
@@ -319,9 +320,13 @@ class EdgeList:
         self.close()
 
 
-def read_edge_list(path: str) -> EdgeList:
+def read_edge_list(path: str, threads: int | None = None) -> EdgeList:
+    """ReadEdgeList semantics; `threads` host threads (None: automatic)."""
     h = _P()
-    _check(_lib.kclpp_read_edge_list(os.fsencode(path), C.byref(h)))
+    if threads is None:
+        _check(_lib.kclpp_read_edge_list(os.fsencode(path), C.byref(h)))
+    else:
+        _check(_lib.kclpp_read_edge_list_mt(os.fsencode(path), threads, C.byref(h)))
     return EdgeList(h)
 
 

@@ -11,6 +11,8 @@
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <thread>
+#include <vector>
 
 #include "kclpp_internal.h"
 
@@ -229,56 +231,130 @@ kclpp_status kclpp_generate(const kclpp_gen_params *p, kclpp_edge_list **out) {
   return KCLPP_OK;
 }
 
-kclpp_status kclpp_read_edge_list(const char *path, kclpp_edge_list **out) {
-  if (!path || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_read_edge_list: null argument");
-  *out = nullptr;
-  FILE *f = fopen(path, "r");
-  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s", path);
-  auto *el = new kclpp_edge_list();
-  // A hand-rolled scanner: same accepted grammar as fscanf("%u %u") on
-  // whitespace-separated decimal pairs, several times faster.
-  std::vector<char> buf(1 << 22);
-  uint32_t mx = 0;
+// Edge-list text parsing (ReadEdgeList, Graph.c:34-53: fscanf("%u %u") until it
+// fails): whitespace-separated decimal numbers, read in pairs; reading stops
+// at the first character that is neither a digit nor whitespace, or at a
+// number above 2^32 - 1.  A number that such a character ends, and a last
+// unpaired number, are dropped; a number that the end of the file ends counts.
+namespace {
+
+inline bool is_space(char c) { return c == ' ' || c == '\n' || c == '\t' || c == '\r'; }
+
+// Numbers of buf[lo, hi) (hi is a whitespace position or the end of the
+// file).  Returns false if the chunk holds a stop (bad character or
+// overflow); the numbers before the stop are kept.
+bool scan_chunk(const char *buf, size_t lo, size_t hi, bool at_eof, std::vector<uint32_t> &out) {
   uint64_t cur = 0;
   bool innum = false;
-  size_t got;
-  int field = 0;
-  uint32_t first = 0;
-  bool bad = false;
-  while ((got = fread(buf.data(), 1, buf.size(), f)) > 0 && !bad) {
-    for (size_t i = 0; i < got; ++i) {
-      char c = buf[i];
-      if (c >= '0' && c <= '9') {
-        cur = cur * 10 + (uint64_t)(c - '0');
-        if (cur > 0xFFFFFFFFull) { bad = true; break; }
-        innum = true;
-      } else if (c == ' ' || c == '\n' || c == '\t' || c == '\r') {
-        if (innum) {
-          if (field == 0) { first = (uint32_t)cur; field = 1; }
-          else {
-            el->pairs.push_back(first);
-            el->pairs.push_back((uint32_t)cur);
-            mx = std::max(mx, std::max(first, (uint32_t)cur));
-            field = 0;
-          }
-          cur = 0;
-          innum = false;
-        }
-      } else {
-        bad = true;  // fscanf would stop reading here
-        break;
-      }
+  for (size_t i = lo; i < hi; ++i) {
+    const char c = buf[i];
+    if (c >= '0' && c <= '9') {
+      cur = cur * 10 + (uint64_t)(c - '0');
+      if (cur > 0xFFFFFFFFull) return false;
+      innum = true;
+    } else if (is_space(c)) {
+      if (innum) out.push_back((uint32_t)cur);
+      cur = 0;
+      innum = false;
+    } else {
+      return false;
     }
   }
-  if (innum && field == 1 && !bad) {
-    el->pairs.push_back(first);
-    el->pairs.push_back((uint32_t)cur);
-    mx = std::max(mx, std::max(first, (uint32_t)cur));
+  // hi is whitespace (the next chunk starts there) or the end of the file
+  if (innum) out.push_back((uint32_t)cur);
+  (void)at_eof;
+  return true;
+}
+
+}  // namespace
+
+kclpp_status kclpp_read_edge_list_mt(const char *path, int threads, kclpp_edge_list **out) {
+  if (!path || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_read_edge_list: null argument");
+  *out = nullptr;
+  FILE *f = fopen(path, "rb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s", path);
+  std::vector<char> buf;
+  long len = -1;
+  if (fseek(f, 0, SEEK_END) == 0) {
+    len = ftell(f);
+    fseek(f, 0, SEEK_SET);
+  }
+  if (len > 0) {  // one read into a buffer of the file's size, then whatever follows
+    buf.resize((size_t)len);
+    buf.resize(fread(buf.data(), 1, buf.size(), f));
+  }
+  {
+    std::vector<char> chunk(1 << 20);
+    size_t got;
+    while ((got = fread(chunk.data(), 1, chunk.size(), f)) > 0) buf.insert(buf.end(), chunk.data(), chunk.data() + got);
   }
   fclose(f);
-  el->n = mx + 1;
+  const size_t size = buf.size();
+  if (threads <= 0) {
+    const unsigned hc = std::thread::hardware_concurrency();
+    threads = size < (8u << 20) ? 1 : (int)std::min<unsigned>(hc ? hc : 1, 16);
+  }
+  // Chunk starts at whitespace positions, so that no number spans two chunks.
+  std::vector<size_t> cut{0};
+  for (int t = 1; t < threads; ++t) {
+    size_t p = std::max(cut.back(), size * (size_t)t / (size_t)threads);
+    while (p < size && !is_space(buf[p])) ++p;
+    if (p >= size) break;
+    if (p > cut.back()) cut.push_back(p);
+  }
+  cut.push_back(size);
+  const size_t nc = cut.size() - 1;
+  std::vector<std::vector<uint32_t>> nums(nc);
+  std::vector<char> clean(nc, 1);
+  auto scan = [&](size_t c) {
+    nums[c].reserve((cut[c + 1] - cut[c]) / 6 + 16);
+    clean[c] = scan_chunk(buf.data(), cut[c], cut[c + 1], c + 1 == nc, nums[c]);
+  };
+  if (nc == 1) {
+    scan(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (size_t c = 0; c < nc; ++c) pool.emplace_back(scan, c);
+    for (auto &th : pool) th.join();
+  }
+  // The numbers up to the first stop, paired in order.
+  size_t used = nc, total = 0;
+  for (size_t c = 0; c < nc; ++c) {
+    total += nums[c].size();
+    if (!clean[c]) { used = c + 1; break; }
+  }
+  const size_t np = total / 2;
+  auto *el = new kclpp_edge_list();
+  el->pairs.resize(2 * np);
+  std::vector<size_t> at(used + 1, 0);
+  for (size_t c = 0; c < used; ++c) at[c + 1] = std::min(at[c] + nums[c].size(), 2 * np);
+  std::vector<uint32_t> mxs(used, 0);
+  auto place = [&](size_t c) {
+    const size_t take = at[c + 1] - at[c];
+    uint32_t m = 0;
+    for (size_t i = 0; i < take; ++i) {
+      const uint32_t v = nums[c][i];
+      el->pairs[at[c] + i] = v;
+      m = v > m ? v : m;
+    }
+    mxs[c] = m;
+  };
+  if (used == 1) {
+    place(0);
+  } else {
+    std::vector<std::thread> pool;
+    for (size_t c = 0; c < used; ++c) pool.emplace_back(place, c);
+    for (auto &th : pool) th.join();
+  }
+  uint32_t mx = 0;
+  for (uint32_t m : mxs) mx = std::max(mx, m);
+  el->n = np ? mx + 1 : 1;
   *out = el;
   return KCLPP_OK;
+}
+
+kclpp_status kclpp_read_edge_list(const char *path, kclpp_edge_list **out) {
+  return kclpp_read_edge_list_mt(path, 0, out);
 }
 
 kclpp_status kclpp_edge_list_create(const uint32_t *pairs, uint64_t e, kclpp_edge_list **out) {

@@ -173,3 +173,56 @@ def test_checkpoint_roundtrip_and_damage(tmp_path):
         assert e.value.status == K.ERR_IO
     with pytest.raises(K.KclppError):
         K.load_state(str(tmp_path / "missing.bin"))
+
+
+def _read_ref(text: str):
+    """The one-pass reading rule of ReadEdgeList (fscanf("%u %u") until it fails)."""
+    nums, cur, innum, bad = [], 0, False, False
+    for ch in text:
+        if "0" <= ch <= "9":
+            cur = cur * 10 + ord(ch) - 48
+            if cur > 0xFFFFFFFF:
+                bad = True
+                break
+            innum = True
+        elif ch in " \n\t\r":
+            if innum:
+                nums.append(cur)
+            cur, innum = 0, False
+        else:
+            bad = True
+            break
+    if innum and not bad:
+        nums.append(cur)
+    return nums[: 2 * (len(nums) // 2)]
+
+
+def test_threaded_reader_matches_one_pass(tmp_path):
+    """kclpp_read_edge_list_mt gives the one-pass result for every thread
+    count, whatever stops the file: a stray character, a number above 2^32-1,
+    an unpaired last number, a number the end of the file ends."""
+    rng = np.random.default_rng(11)
+    seps = [" ", "\n", "\t", "\r\n", "  ", "\n\n"]
+    for case in range(40):
+        m = int(rng.integers(0, 3000))
+        toks = [str(int(x)) for x in rng.integers(0, 1 << 20, size=2 * m)]
+        text = "".join(t + seps[int(rng.integers(0, len(seps)))] for t in toks)
+        kind = case % 5
+        if kind == 1 and text:
+            p = int(rng.integers(0, len(text)))
+            text = text[:p] + "#" + text[p:]
+        elif kind == 2 and text:
+            p = int(rng.integers(0, len(text)))
+            text = text[:p] + " 99999999999 " + text[p:]
+        elif kind == 3:
+            text = text + "17"
+        elif kind == 4:
+            text = text.rstrip() + " 5 6"
+        f = tmp_path / f"e{case}.txt"
+        f.write_bytes(text.encode())
+        want = np.array(_read_ref(text), dtype=np.uint32).reshape(-1, 2)
+        for th in (1, 2, 3, 7, 16):
+            el = K.read_edge_list(str(f), threads=th)
+            got = el.pairs()
+            assert np.array_equal(got, want), (case, th)
+            assert el.n == (int(want.max()) + 1 if len(want) else 1)
