@@ -84,6 +84,11 @@ kclpp_status kclpp_read_edge_list(const char *path, kclpp_edge_list **out);
  * identical results for any count (the numbers are split at whitespace and
  * the first stop ends the file, as in the one-thread scan). */
 kclpp_status kclpp_read_edge_list_mt(const char *path, int threads, kclpp_edge_list **out);
+/* Binary edge lists (no reference counterpart): a checksummed cache of a
+ * parsed file -- n, the pairs in input order -- read back without parsing.  A
+ * truncated or altered file returns KCLPP_ERR_IO. */
+kclpp_status kclpp_write_edge_list_bin(const kclpp_edge_list *el, const char *path);
+kclpp_status kclpp_read_edge_list_bin(const char *path, kclpp_edge_list **out);
 /* pairs = s0 t0 s1 t1 ... (2*e entries); n = max id + 1 as in ReadEdgeList. */
 kclpp_status kclpp_edge_list_create(const uint32_t *pairs, uint64_t e, kclpp_edge_list **out);
 kclpp_status kclpp_edge_list_info(const kclpp_edge_list *el, uint32_t *n, uint64_t *e);

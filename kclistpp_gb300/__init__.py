@@ -134,6 +134,8 @@ _SIGS = {
     "kclpp_profile_read": (C.c_int, [_P, C.POINTER(KernelTime), C.c_int, C.POINTER(C.c_int)]),
     "kclpp_read_edge_list": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "kclpp_read_edge_list_mt": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
+    "kclpp_write_edge_list_bin": (C.c_int, [_P, C.c_char_p]),
+    "kclpp_read_edge_list_bin": (C.c_int, [C.c_char_p, C.POINTER(_P)]),
     "kclpp_edge_list_create": (C.c_int, [_u32p, C.c_uint64, C.POINTER(_P)]),
     "kclpp_edge_list_info": (C.c_int, [_P, _u32p, _u64p]),
     "kclpp_edge_list_copy": (C.c_int, [_P, _u32p]),
@@ -304,6 +306,15 @@ class EdgeList:
 
     def write(self, path: str) -> None:
         _check(_lib.kclpp_write_edge_list(self._h, os.fsencode(path)))
+
+    def write_bin(self, path: str) -> None:
+        _check(_lib.kclpp_write_edge_list_bin(self._h, os.fsencode(path)))
+
+    @classmethod
+    def read_bin(cls, path: str) -> "EdgeList":
+        h = _P()
+        _check(_lib.kclpp_read_edge_list_bin(os.fsencode(path), C.byref(h)))
+        return cls(h)
 
     def hash(self) -> int:
         """FNV-1a of n and the pairs: the graph_hash of a checkpoint."""

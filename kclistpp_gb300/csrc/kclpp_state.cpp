@@ -105,6 +105,50 @@ kclpp_status kclpp_load_state(const char *path, kclpp_state_info *info, void *ve
   return KCLPP_OK;
 }
 
+// Binary edge lists: "KCLPPEL1", u32 n, u64 e, 2e x u32 pairs, u64 checksum
+// (FNV-1a of every byte before it).  A cache of a parsed text file.
+kclpp_status kclpp_write_edge_list_bin(const kclpp_edge_list *el, const char *path) {
+  if (!el || !path) return set_error(KCLPP_ERR_INVALID, "kclpp_write_edge_list_bin: null argument");
+  const uint64_t e = el->e();
+  std::vector<unsigned char> buf(8 + 4 + 8 + (size_t)e * 8 + 8);
+  memcpy(buf.data(), "KCLPPEL1", 8);
+  put32(&buf[8], el->n);
+  put64(&buf[12], e);
+  for (size_t i = 0; i < el->pairs.size(); ++i) put32(&buf[20 + 4 * i], el->pairs[i]);
+  put64(&buf[buf.size() - 8], fnv1a(buf.data(), buf.size() - 8));
+  FILE *f = fopen(path, "wb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s for writing", path);
+  const size_t w = fwrite(buf.data(), 1, buf.size(), f);
+  const int rc = fclose(f);
+  if (w != buf.size() || rc != 0) return set_error(KCLPP_ERR_IO, "write failed: %s", path);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_read_edge_list_bin(const char *path, kclpp_edge_list **out) {
+  if (!path || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_read_edge_list_bin: null argument");
+  *out = nullptr;
+  FILE *f = fopen(path, "rb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s", path);
+  std::vector<unsigned char> buf;
+  unsigned char chunk[1 << 16];
+  size_t got;
+  while ((got = fread(chunk, 1, sizeof chunk, f)) > 0) buf.insert(buf.end(), chunk, chunk + got);
+  fclose(f);
+  if (buf.size() < 28 || memcmp(buf.data(), "KCLPPEL1", 8) != 0)
+    return set_error(KCLPP_ERR_IO, "%s is not a binary kclpp edge list", path);
+  const uint64_t e = get64(&buf[12]);
+  if (e > (buf.size() - 28) / 8 || buf.size() != 28 + (size_t)e * 8)
+    return set_error(KCLPP_ERR_IO, "%s: truncated edge list", path);
+  if (get64(&buf[buf.size() - 8]) != fnv1a(buf.data(), buf.size() - 8))
+    return set_error(KCLPP_ERR_IO, "%s: checksum mismatch", path);
+  auto *el = new kclpp_edge_list();
+  el->n = get32(&buf[8]);
+  el->pairs.resize((size_t)e * 2);
+  for (size_t i = 0; i < el->pairs.size(); ++i) el->pairs[i] = get32(&buf[20 + 4 * i]);
+  *out = el;
+  return KCLPP_OK;
+}
+
 kclpp_status kclpp_edge_list_hash(const kclpp_edge_list *el, uint64_t *hash) {
   if (!el || !hash) return set_error(KCLPP_ERR_INVALID, "kclpp_edge_list_hash: null argument");
   std::vector<unsigned char> b(8 + el->pairs.size() * 4);

@@ -226,3 +226,20 @@ def test_threaded_reader_matches_one_pass(tmp_path):
             got = el.pairs()
             assert np.array_equal(got, want), (case, th)
             assert el.n == (int(want.max()) + 1 if len(want) else 1)
+
+
+def test_binary_edge_list_cache(tmp_path):
+    """A parsed edge list written in binary reads back identical (n and the
+    pairs in input order); a damaged file is refused."""
+    el = K.rmat(12, 16, seed=5)
+    p = str(tmp_path / "g.bin")
+    el.write_bin(p)
+    back = K.EdgeList.read_bin(p)
+    assert back.n == el.n and np.array_equal(back.pairs(), el.pairs())
+    raw = open(p, "rb").read()
+    for bad in (raw[:-1], raw[:30], raw[:25] + bytes([raw[25] ^ 4]) + raw[26:], b"X" + raw[1:]):
+        q = str(tmp_path / "bad.bin")
+        open(q, "wb").write(bad)
+        with pytest.raises(K.KclppError) as e:
+            K.EdgeList.read_bin(q)
+        assert e.value.status == K.ERR_IO
