@@ -271,6 +271,23 @@ kclpp_status kclpp_sim_passes_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const 
                                   const uint32_t *cols, int k, uint32_t t_first, uint32_t passes,
                                   double *rho_inout);
 
+/* ---- exact k-clique densest subgraph (host; the reference's certifier,
+ * MaxFlow.cpp / kCDensestMem.c, needs Boost, which this build does not use).
+ * The published max-flow construction for the k-clique densest subgraph
+ * (Goldberg's network with a node per (k-1)-clique), solved by Dinic's
+ * algorithm and iterated from the whole graph's density to the optimum.  For
+ * graphs with up to 2e7 k-cliques (KCLPP_ERR_UNSUPPORTED beyond); members, if
+ * not NULL, gets n flags (original ids) marking one densest set. */
+typedef struct {
+  uint64_t num, den;       /* the optimum density num / den, reduced          */
+  double density;
+  uint32_t size;           /* vertices of the densest set found               */
+  uint64_t cliques;        /* its k-cliques (cliques / size = num / den)      */
+  uint64_t cliques_total;  /* k-cliques of the graph                          */
+  int iterations;          /* max-flow solves                                 */
+} kclpp_exact_info;
+kclpp_status kclpp_densest_exact(const kclpp_edge_list *el, int k, kclpp_exact_info *info, uint8_t *members);
+
 /* ---- checkpoints (no reference counterpart: its dump of r is commented out,
  * kCDensestNoAtom.c:398-401).  Host only: a run's vector -- Seq r (u64) or
  * Sim rho (f64, by bit pattern) -- with the passes done, k and a hash of its

@@ -70,6 +70,11 @@ class StateInfo(C.Structure):
                 ("graph_hash", C.c_uint64)]
 
 
+class ExactInfo(C.Structure):
+    _fields_ = [("num", C.c_uint64), ("den", C.c_uint64), ("density", C.c_double), ("size", C.c_uint32),
+                ("cliques", C.c_uint64), ("cliques_total", C.c_uint64), ("iterations", C.c_int)]
+
+
 class KernelTime(C.Structure):
     _fields_ = [("mode", C.c_int), ("tier", C.c_int), ("dmax", C.c_uint32), ("launches", C.c_uint32),
                 ("ms", C.c_double)]
@@ -140,6 +145,7 @@ _SIGS = {
     "kclpp_edge_list_info": (C.c_int, [_P, _u32p, _u64p]),
     "kclpp_edge_list_copy": (C.c_int, [_P, _u32p]),
     "kclpp_write_edge_list": (C.c_int, [_P, C.c_char_p]),
+    "kclpp_densest_exact": (C.c_int, [_P, C.c_int, _P, _P]),
     "kclpp_save_state": (C.c_int, [C.c_char_p, _P, _P]),
     "kclpp_load_state": (C.c_int, [C.c_char_p, _P, _P, C.c_uint32]),
     "kclpp_edge_list_hash": (C.c_int, [_P, _u64p]),
@@ -694,3 +700,12 @@ def load_state(path: str) -> tuple[StateInfo, np.ndarray]:
     v = np.empty(info.n, dtype=np.uint64 if info.kind == KERNEL_SEQ else np.float64)
     _check(_lib.kclpp_load_state(os.fsencode(path), C.byref(info), v.ctypes.data_as(_P), info.n))
     return info, v
+
+
+def densest_exact(el: EdgeList, k: int) -> tuple[ExactInfo, np.ndarray]:
+    """Exact k-clique densest subgraph of a small graph (host max-flow): the
+    optimum as a fraction, and a boolean mask of one densest vertex set."""
+    info = ExactInfo()
+    mask = np.zeros(max(el.n, 1), dtype=np.uint8)
+    _check(_lib.kclpp_densest_exact(el._h, k, C.byref(info), mask.ctypes.data_as(_P)))
+    return info, mask[: el.n].astype(bool)

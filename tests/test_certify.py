@@ -139,3 +139,45 @@ def test_library_certificates_bracket_the_optimum(ctx, gi):
         assert info.density <= rho * (1 + 1e-12) and info.ub >= rho * (1 - 1e-12)
         info, _ = K.extract_densest_seq(g, k, T, K.seq_passes(g, k, T))
         assert info.density <= rho * (1 + 1e-12) and info.ub >= rho * (1 - 1e-12)
+
+
+@pytest.mark.parametrize("gi,k", [(i, k) for i in range(len(_small_graphs())) for k in (2, 3, 4)])
+def test_exact_densest_matches_every_subset(gi, k):
+    """kclpp_densest_exact (host max-flow) against trying every vertex subset:
+    the same optimum as a fraction, and a vertex set that attains it."""
+    from fractions import Fraction
+
+    n, pairs = _small_graphs()[gi]
+    masks = _cliques(n, pairs, k)
+    el = K.EdgeList.from_pairs(pairs)
+    info, members = K.densest_exact(el, k)
+    if len(masks) == 0:
+        assert info.cliques_total == 0
+        return
+    num, den = _rho_star(n, masks)
+    assert Fraction(info.num, info.den) == Fraction(num, den)
+    assert info.cliques_total == len(masks)
+    S = sum(1 << int(v) for v in np.nonzero(members)[0])
+    inside = int(((masks & ~S) == 0).sum())
+    assert members.sum() == info.size and inside == info.cliques
+    assert Fraction(inside, int(members.sum())) == Fraction(num, den)
+
+
+@pytest.mark.parametrize("name,k", [("config1_chung_lu_1e4", 3), ("config1_chung_lu_1e4", 4), ("planted_3000", 4),
+                                    ("cl_2000", 3), ("cl_2000", 4)])
+def test_seq_result_is_the_certified_optimum(name, k):
+    """On the golden graphs (config 1: Chung-Lu n = 1e4, average degree 20,
+    exponent 2.5, seed 1), the densest prefix Seq-kClist++ reports after 64
+    passes is the exact optimum that the max-flow certifier proves, and the
+    reported upper bound lies above it."""
+    from fractions import Fraction
+
+    from tests import golden_util as Gu
+
+    P = Gu.pairs(name)
+    info, members = K.densest_exact(K.EdgeList.from_pairs(P), k)
+    infos, _ = O.Graph(P).seq_main(k, 64, mode=O.SEQ_EDGE_STREAMS)
+    last = infos[-1]
+    assert Fraction(last.cliques, last.n) == Fraction(info.num, info.den)
+    assert last.ub >= info.density
+    assert info.iterations >= 1 and members.sum() == info.size
