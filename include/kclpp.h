@@ -426,7 +426,10 @@ typedef struct {
   uint64_t ncktrim;      /* k-cliques kept                                     */
 } kclpp_trim_info;
 /* main of kClistCoreTrim.c:707-775: kcore (:242-272), relabelnodes (:274-294),
- * mkspecial (:306-331), onepass (:394-416), kcliquecore (:605-666). */
+ * mkspecial (:306-331), onepass (:394-416), kcliquecore (:605-666).  k = 2 is
+ * NormalGraphCoreTrim.c (TrimByCoreDecomp, :41-110): a host-only degree peel
+ * (ctx may be NULL); its statistics are ntrim, mtrim = ncktrim, and ckrho =
+ * rho = the best edge density along the peel; map is the identity. */
 kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int k, int mode,
                         kclpp_trim_result **out);
 kclpp_status kclpp_trim_info_get(const kclpp_trim_result *t, kclpp_trim_info *info);

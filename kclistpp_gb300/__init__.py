@@ -664,9 +664,10 @@ class TrimResult:
     edges: EdgeList        # trimmed graph, original ids, input order
 
 
-def trim(ctx: Context, el: EdgeList, k: int, mode: int = TRIM_EXACT) -> TrimResult:
+def trim(ctx: Context | None, el: EdgeList, k: int, mode: int = TRIM_EXACT) -> TrimResult:
+    """The k-clique core trim; k = 2 runs on the host alone (ctx may be None)."""
     h = _P()
-    _check(_lib.kclpp_trim(ctx.handle, el._h, k, mode, C.byref(h)))
+    _check(_lib.kclpp_trim(ctx.handle if ctx is not None else None, el._h, k, mode, C.byref(h)))
     try:
         info = TrimInfo()
         _check(_lib.kclpp_trim_info_get(h, C.byref(info)))

@@ -35,7 +35,7 @@ NVCCFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr"
 
 CU_SOURCES = ["kclpp_api.cu", "kclpp_k_count.cu", "kclpp_k_order.cu", "kclpp_k_seq.cu", "kclpp_warm.cu"]
 CPP_SOURCES = ["kclpp_gen.cpp", "kclpp_order.cpp", "kclpp_trim.cpp", "kclpp_state.cpp", "kclpp_exact.cpp"]
-PROGRAMS = ["kCDensestNoAtom", "kCDensestCmpSync", "kClistCoreTrim"]
+PROGRAMS = ["kCDensestNoAtom", "kCDensestCmpSync", "kClistCoreTrim", "NormalGraphCoreTrim"]
 
 
 def _newer(target: str, deps: list[str]) -> bool:

@@ -54,6 +54,9 @@ void ctx_count_launch(kclpp_ctx *c, int n);
 
 // SortByCore with the reference heap's tie order.
 void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank);
+// The same peel: vertices in pop order and the degree each had when popped
+// (degree_at_pop may be null).
+void core_peel_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *order, uint64_t *degree_at_pop);
 // Relabel + sort + CSR; fails on self loops or repeated edges.
 kclpp_status make_dag_host(const std::vector<uint32_t> &pairs, const uint32_t *rank, HostDag &dag);
 

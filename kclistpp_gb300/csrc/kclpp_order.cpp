@@ -68,7 +68,7 @@ struct Heap {
 };
 }  // namespace
 
-void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank) {
+void core_peel_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *order, uint64_t *degree_at_pop) {
   const uint64_t e = pairs.size() / 2;
   std::vector<uint64_t> cd((size_t)n + 1, 0);
   for (uint64_t i = 0; i < e; ++i) { cd[pairs[2 * i] + 1]++; cd[pairs[2 * i + 1] + 1]++; }
@@ -82,12 +82,19 @@ void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *r
   }
   Heap h(n);
   for (uint32_t i = 0; i < n; ++i) h.push(i, cd[i + 1] - cd[i]);
-  uint32_t r = 0;
   for (uint32_t i = 0; i < n; ++i) {
-    uint32_t k = h.pop(nullptr);
-    rank[k] = n - (++r);
+    uint64_t v = 0;
+    const uint32_t k = h.pop(&v);
+    order[i] = k;
+    if (degree_at_pop) degree_at_pop[i] = v;
     for (uint64_t j = cd[k]; j < cd[k + 1]; ++j) h.dec(adj[j], 1);
   }
+}
+
+void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank) {
+  std::vector<uint32_t> order(n);
+  core_peel_host(n, pairs, order.data(), nullptr);
+  for (uint32_t i = 0; i < n; ++i) rank[order[i]] = n - 1 - i;  // rank = n - (pops so far)
 }
 
 kclpp_status make_dag_host(const std::vector<uint32_t> &pairs, const uint32_t *rank, HostDag &dag) {

@@ -117,11 +117,72 @@ struct Rec {
 
 extern "C" {
 
+// k = 2 (NormalGraphCoreTrim.c, TrimByCoreDecomp :41-110): the degree peel of
+// SortByCore; the best edge density along it is max_rho, and vertices are
+// dropped in peel order while the degree they had when peeled is below it.
+// Host only: the 2-cliques are the edges.
+static kclpp_status trim_k2(const kclpp_edge_list *el, kclpp_trim_result **out) {
+  std::unique_ptr<kclpp_trim_result> R(new kclpp_trim_result());
+  kclpp_trim_info &I = R->info;
+  memset(&I, 0, sizeof I);
+  const uint32_t n = el->n;
+  const uint64_t e = el->e();
+  const std::vector<uint32_t> &P = el->pairs;
+  I.n = I.n2 = n;
+  I.e = I.e2 = e;
+  I.total = e;
+  std::vector<uint32_t> order(n);
+  std::vector<uint64_t> at_pop(n);
+  core_peel_host(n, P, order.data(), at_pop.data());
+  double max_rho = -1;
+  uint64_t cnt = e, core = 0;
+  R->core_num.resize(n);
+  for (uint32_t i = 0; i < n; ++i) {
+    if (max_rho < (double)cnt / (double)(n - i)) {
+      max_rho = (double)cnt / (double)(n - i);
+      I.size = n - i;
+    }
+    cnt -= at_pop[i];
+    core = std::max(core, at_pop[i]);
+    R->core_num[i] = core;
+  }
+  I.core = (uint32_t)core;
+  I.ckcore = core;
+  I.ckrho = I.rho = max_rho;
+  std::vector<char> alive(n, 1);
+  cnt = e;
+  for (uint32_t i = 0; i < n; ++i) {
+    if ((double)at_pop[i] < max_rho) {
+      alive[order[i]] = 0;
+      cnt -= at_pop[i];
+    } else {
+      I.ntrim = n - i;
+      I.mtrim = I.ncktrim = cnt;
+      break;
+    }
+  }
+  R->map.resize(n);
+  R->nck.assign(n, 0);
+  for (uint32_t v = 0; v < n; ++v) R->map[v] = v;
+  for (uint64_t i = 0; i < e; ++i) { R->nck[P[2 * i]]++; R->nck[P[2 * i + 1]]++; }
+  R->order = order;
+  for (uint64_t i = 0; i < e; ++i)
+    if (alive[P[2 * i]] && alive[P[2 * i + 1]]) {
+      R->trimmed.push_back(P[2 * i]);
+      R->trimmed.push_back(P[2 * i + 1]);
+    }
+  *out = R.release();
+  return KCLPP_OK;
+}
+
 kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int mode, kclpp_trim_result **out) {
-  if (!ctx || !el || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_trim: null argument");
+  if (!el || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_trim: null argument");
   *out = nullptr;
+  if (mode != KCLPP_TRIM_EXACT && mode != KCLPP_TRIM_FAST) return set_error(KCLPP_ERR_INVALID, "unknown trim mode");
+  if (kmax == 2) return trim_k2(el, out);
+  if (!ctx) return set_error(KCLPP_ERR_INVALID, "kclpp_trim: null context (needed for k >= 3)");
   if (kmax < 3 || kmax > KCLPP_MAX_K)
-    return set_error(KCLPP_ERR_UNSUPPORTED, "k = %d outside [3, %d]", kmax, KCLPP_MAX_K);
+    return set_error(KCLPP_ERR_UNSUPPORTED, "k = %d outside [2, %d]", kmax, KCLPP_MAX_K);
   if (mode != KCLPP_TRIM_EXACT && mode != KCLPP_TRIM_FAST) return set_error(KCLPP_ERR_INVALID, "unknown trim mode");
   std::unique_ptr<kclpp_trim_result> R(new kclpp_trim_result());
   kclpp_trim_info &I = R->info;

@@ -243,3 +243,43 @@ def test_binary_edge_list_cache(tmp_path):
         with pytest.raises(K.KclppError) as e:
             K.EdgeList.read_bin(q)
         assert e.value.status == K.ERR_IO
+
+
+def test_trim_k2_matches_reference():
+    """k = 2 (NormalGraphCoreTrim.c): vertices kept, edges kept and the trimmed
+    edge list, in input order, equal to the reference program's output files
+    on every golden graph (tests/golden/make_golden_trim2.py); host only."""
+    import json
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    index = json.load(open(os.path.join(here, "trim2.json")))
+    arrays = np.load(os.path.join(here, "trim2.npz"))
+    graphs = {name: G.pairs(name) for name in G.index()}
+    graphs["planted_k2"] = K.planted(4000, 6.0, 2.2, 2, 40, 90, 0.5, seed=21).pairs()
+    graphs["chung_lu_k2"] = K.chung_lu(5000, 12.0, 2.2, seed=22).pairs()
+    assert set(index) == set(graphs)
+    for name, meta in index.items():
+        pairs = np.ascontiguousarray(graphs[name], dtype=np.uint32)
+        assert hashlib.sha256(pairs.tobytes()).hexdigest() == meta["sha256"], name
+        tr = K.trim(None, K.EdgeList.from_pairs(pairs), 2)
+        assert (tr.info.ntrim, tr.info.mtrim, tr.info.ncktrim) == (meta["ntrim"], meta["mtrim"], meta["ncktrim"]), name
+        assert np.array_equal(tr.edges.pairs(), arrays[f"{name}_trimmed"]), name
+
+
+def test_normal_graph_core_trim_cli(tmp_path):
+    """The drop-in NormalGraphCoreTrim program writes the reference's two files
+    (trimmed edges, statistics) for a golden graph; no GPU is used."""
+    import json
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    meta = json.load(open(os.path.join(here, "trim2.json")))["cl_2000"]
+    want = np.load(os.path.join(here, "trim2.npz"))["cl_2000_trimmed"]
+    exe = os.path.join(os.path.dirname(K.LIB_PATH), "bin", "NormalGraphCoreTrim")
+    edges = tmp_path / "g.txt"
+    edges.write_text("".join(f"{s} {t}\n" for s, t in G.pairs("cl_2000")))
+    subprocess.run([exe, str(edges), "x"], cwd=tmp_path, check=True, capture_output=True)
+    got = np.loadtxt(tmp_path / "trimmed_x_2.txt", dtype=np.uint32, ndmin=2).reshape(-1, 2)
+    assert np.array_equal(got, want)
+    stat = (tmp_path / "stat_trim_x_2.txt").read_text().split("\n")
+    assert stat[0].startswith("[Number of Nodes]")
+    assert [int(x) for x in stat[1].split("\t")[:3]] == [meta["ntrim"], meta["mtrim"], meta["ncktrim"]]
