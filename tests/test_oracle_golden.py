@@ -103,3 +103,21 @@ def test_seq_waves_restatement(name, k, T):
         got = g.seq_pass_waves(k, r0, waves)
         assert np.array_equal(got, r)
         assert int((got - r0).sum()) == tot
+
+
+def test_sim_k2_matches_reference():
+    """Sim-kClist++ at k = 2 (the edge branch, kCDensestCmpSync.c:189-192): the
+    oracle's reports and FP64 rho equal the reference's, bit for bit, on every
+    golden graph (tests/golden/make_golden_sim2.py)."""
+    import json
+    import os
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    index = json.load(open(os.path.join(here, "sim2.json")))
+    arrays = np.load(os.path.join(here, "sim2.npz"))
+    for name, meta in index.items():
+        g = O.Graph(G.pairs(name))
+        infos, rho = g.sim_main(2, meta["T"])
+        want = [[i[0], i[1], i[2], float.fromhex(i[3]), float.fromhex(i[4])] for i in meta["infos"]]
+        assert G.infos_equal(want, infos), name
+        assert np.array_equal(rho.view(np.uint64), arrays[f"{name}_rho_bits"]), name
