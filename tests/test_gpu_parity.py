@@ -293,3 +293,20 @@ def test_complete_graph_known_answers(ctx):
         assert int(r.sum()) == comb(10, k)
         infos, _ = K.sim_main(g, k, 4)
         assert infos[-1].n == 10 and infos[-1].cliques == comb(10, k)
+
+
+def test_sim_k2_matches_reference(ctx):
+    """Sim-kClist++ at k = 2 (kCDensestCmpSync.c:189-192): reports and FP64 rho
+    bit-identical to the reference's on every golden graph."""
+    import json
+    import os
+
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    index = json.load(open(os.path.join(here, "sim2.json")))
+    arrays = np.load(os.path.join(here, "sim2.npz"))
+    for name, meta in index.items():
+        g = dev_graph(ctx, G.pairs(name))
+        infos, rho = K.sim_main(g, 2, meta["T"])
+        want = [[i[0], i[1], i[2], float.fromhex(i[3]), float.fromhex(i[4])] for i in meta["infos"]]
+        assert G.infos_equal(want, infos), name
+        assert np.array_equal(bits(rho), arrays[f"{name}_rho_bits"]), name
