@@ -243,7 +243,7 @@ inline bool is_space(char c) { return c == ' ' || c == '\n' || c == '\t' || c ==
 // Numbers of buf[lo, hi) (hi is a whitespace position or the end of the
 // file).  Returns false if the chunk holds a stop (bad character or
 // overflow); the numbers before the stop are kept.
-bool scan_chunk(const char *buf, size_t lo, size_t hi, bool at_eof, std::vector<uint32_t> &out) {
+bool scan_chunk(const char *buf, size_t lo, size_t hi, std::vector<uint32_t> &out) {
   uint64_t cur = 0;
   bool innum = false;
   for (size_t i = lo; i < hi; ++i) {
@@ -262,7 +262,6 @@ bool scan_chunk(const char *buf, size_t lo, size_t hi, bool at_eof, std::vector<
   }
   // hi is whitespace (the next chunk starts there) or the end of the file
   if (innum) out.push_back((uint32_t)cur);
-  (void)at_eof;
   return true;
 }
 
@@ -308,7 +307,7 @@ kclpp_status kclpp_read_edge_list_mt(const char *path, int threads, kclpp_edge_l
   std::vector<char> clean(nc, 1);
   auto scan = [&](size_t c) {
     nums[c].reserve((cut[c + 1] - cut[c]) / 6 + 16);
-    clean[c] = scan_chunk(buf.data(), cut[c], cut[c + 1], c + 1 == nc, nums[c]);
+    clean[c] = scan_chunk(buf.data(), cut[c], cut[c + 1], nums[c]);
   };
   if (nc == 1) {
     scan(0);
