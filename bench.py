@@ -18,6 +18,17 @@ root edges of the same workload.
 
 The graph preparation (generation, trim, DAG) is not timed; the trim counts
 cliques on the GPU in both arms.
+
+The JSON line also carries: the pass-level roofline (the reference's
+per-root-edge gather bytes over the Seq pass time, against the measured HBM
+copy bandwidth), the host-buffer run through the C ABI (`e2e`, the same
+passes from the same state), the CPU port's rate (`cpu_baseline`), clocks
+sampled during the timed region, and `convergence`: wall time to a certified
+1 % density gap on a held-out RMAT-16 graph with planted communities (k = 5)
+for the zero start, the learned warm start and the wave ordering
+(`--no-convergence` skips it).  `--workload batch` measures the batched
+configuration instead (many uneven graphs x k = 3..7 in one captured CUDA
+graph) and prints its own line.
 """
 from __future__ import annotations
 
