@@ -181,3 +181,32 @@ def test_seq_result_is_the_certified_optimum(name, k):
     assert Fraction(last.cliques, last.n) == Fraction(info.num, info.den)
     assert last.ub >= info.density
     assert info.iterations >= 1 and members.sum() == info.size
+
+
+def test_random_graphs_certificates_hold():
+    """Random small graphs (hypothesis): the max-flow optimum equals the
+    exhaustive one, and every Seq report brackets it."""
+    hyp = pytest.importorskip("hypothesis")
+    st = pytest.importorskip("hypothesis.strategies")
+    from fractions import Fraction
+
+    @hyp.settings(max_examples=60, deadline=None, derandomize=True)
+    @hyp.given(st.integers(5, 12), st.floats(0.2, 0.9), st.integers(2, 4), st.integers(0, 2**31 - 1))
+    def check(n, p, k, seed):
+        rng = np.random.default_rng(seed)
+        pairs = np.array([(u, v) for u in range(n) for v in range(u + 1, n) if rng.random() < p], dtype=np.uint32)
+        if len(pairs) == 0:
+            return
+        masks = _cliques(n, pairs, k)
+        info, _ = K.densest_exact(K.EdgeList.from_pairs(pairs), k)
+        if len(masks) == 0:
+            assert info.cliques_total == 0
+            return
+        num, den = _rho_star(n, masks)
+        assert Fraction(info.num, info.den) == Fraction(num, den)
+        if k >= 3:
+            infos, _ = O.Graph(pairs).seq_main(k, 16, mode=O.SEQ_EDGE_STREAMS)
+            for inf in infos:
+                assert inf.density <= num / den * (1 + 1e-12) and inf.ub >= num / den * (1 - 1e-12)
+
+    check()
