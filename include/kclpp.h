@@ -442,6 +442,76 @@ kclpp_status kclpp_trim_copy(const kclpp_trim_result *t, uint32_t *map, uint64_t
 kclpp_status kclpp_trim_edges(const kclpp_trim_result *t, kclpp_edge_list **out);
 void kclpp_trim_free(kclpp_trim_result *t);
 
+/* ---- Seq-Sampling++ (kCDensestSamplingKclistpp.c) -------------------------
+ * Keeps a sample of the k-cliques in device memory, runs the "++" passes over
+ * the sample only and reports the densest prefix of the sampled loads, its
+ * exact k-clique count and the scaled upper bound (Solve, :446-489).
+ *
+ * Sampling: p = target / (k-cliques of the graph), at most 1 (:272; the
+ * reference's target is CLIQUES_TO_SAMPLE = 10^7, :138).  Where the reference
+ * draws rand() per clique (:160, :198), a clique Q is kept iff
+ * mix64(sum of key(v), v in Q) < floor(p * 2^64), key(v) = mix64(seed + (v + 1)
+ * * 0x9E3779B97F4A7C15), mix64 = SplitMix64's output function: the same
+ * sample on every run, device and schedule.
+ *
+ * "++" pass: where the reference updates the sample one clique at a time in a
+ * fresh random order (InMemoryFrankWolfe, :345-361), the sample is split into
+ * `waves` fixed groups (by the same key sum); the waves run one after another
+ * and the cliques of a wave all compare the values the earlier waves left
+ * (each gives its unit to its member of smallest value, ties to the smallest
+ * id, as the reference).  waves = 1 is a synchronous pass; results do not
+ * depend on the order in which the GPU visits the cliques.
+ *
+ * The graph must outlive the sampling object.  k in [3, 8], out-degree up to
+ * 2048, target in [1, 2^31 - 1], waves in [1, 256]. */
+#define KCLPP_SAMPLE_TARGET 10000000u
+typedef struct kclpp_sampling kclpp_sampling;
+typedef struct {
+  uint64_t cliques_total; /* k-cliques of the graph (the COUNT task, :153-157)      */
+  uint64_t sampled;       /* cliques kept                                         */
+  double prob;            /* sampling probability (sampling_prob, :272)           */
+  uint64_t threshold;     /* floor(prob * 2^64) (0 when every clique is kept)     */
+  int all;                /* prob = 1: every clique kept                          */
+  uint32_t waves;
+  uint32_t passes;        /* "++" passes applied so far                           */
+} kclpp_sampling_info;
+typedef struct {
+  uint32_t T;             /* passes the loads stand for (ExtractDensest's T)       */
+  uint32_t n;             /* densest prefix by the sampled loads (info.n, :385-394) */
+  uint64_t m;             /* sampled cliques pushed inside it (info.m)              */
+  double density;         /* m / n                                                  */
+  double ub;              /* bound from the sampled loads (info.ub, :400-417)       */
+  uint32_t sub_n;         /* the densest subgraph's vertices with an edge (:467-470) */
+  uint64_t sub_e;         /* its edges                                              */
+  uint32_t sub_core;      /* its core value (max out-degree of its DAG)             */
+  uint64_t sub_cliques;   /* its k-cliques, counted exactly on the GPU (:471)       */
+  double edge_density;    /* sub_e * 2.0 / sub_n / (sub_n - 1)         (:475)       */
+  double clique_density;  /* sub_cliques / sub_n                       (:476)       */
+  double upper_bound;     /* ub / prob / (1 - sqrt(6 ln n / ub))       (:477)       */
+} kclpp_sampling_report;
+/* KCLIST_CliqueEnum COUNT then SAMPLING (SampleCliques, :438-444). */
+kclpp_status kclpp_sampling_create(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint64_t target, uint64_t seed,
+                                   uint32_t waves, kclpp_sampling **out);
+kclpp_status kclpp_sampling_info_get(const kclpp_sampling *s, kclpp_sampling_info *info);
+/* The kept cliques, k ascending ids per row (the ck[] rows, :160-170), rows in
+ * lexicographic order of (largest member, next largest, ...); waves gets each
+ * row's wave.  rows holds sampled * k ids; either output may be NULL. */
+kclpp_status kclpp_sampling_cliques(kclpp_ctx *ctx, const kclpp_sampling *s, uint32_t *rows, uint8_t *waves);
+kclpp_status kclpp_sampling_passes(kclpp_ctx *ctx, kclpp_sampling *s, uint32_t passes);
+/* The loads (rho, u32 per vertex, :328) and the passes they stand for. */
+kclpp_status kclpp_sampling_get_rho(kclpp_ctx *ctx, const kclpp_sampling *s, uint32_t *rho);
+kclpp_status kclpp_sampling_set_rho(kclpp_ctx *ctx, kclpp_sampling *s, const uint32_t *rho, uint32_t passes);
+/* ExtractDensest (:364-419) for loads that stand for T passes, then the exact
+ * count in the densest prefix's induced subgraph (:420-435, :467-471).  order, if not
+ * NULL, gets the n vertices by decreasing load (ties: ascending id). */
+kclpp_status kclpp_sampling_extract(kclpp_ctx *ctx, kclpp_sampling *s, uint32_t T, kclpp_sampling_report *rep,
+                                    uint32_t *order);
+void kclpp_sampling_free(kclpp_sampling *s);
+/* Solve (:444-489): sample, then passes 1..2^floor(log2 num_iter) with one
+ * report per power of two (cap reports at most; *count gets how many). */
+kclpp_status kclpp_sampling_main(kclpp_ctx *ctx, const kclpp_graph *g, int k, uint32_t num_iter, uint64_t target,
+                                 uint64_t seed, uint32_t waves, kclpp_sampling_report *reps, int cap, int *count);
+
 #ifdef __cplusplus
 }
 #endif

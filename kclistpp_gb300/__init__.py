@@ -16,6 +16,9 @@ functions (btsun/kclistpp):
     extract_densest_*   CDF_FindDensestSubset         kCDensestNoAtom.c:330-371
     seq_main/sim_main   CDF_Main                      kCDensestNoAtom.c:373-402
     trim                kClistCoreTrim main           kClistCoreTrim.c:707-775
+    Sampling            SampleCliques / InMemoryFrankWolfe / ExtractDensest
+                                                  kCDensestSamplingKclistpp.c:345-444
+    sampling_main       Solve                         kCDensestSamplingKclistpp.c:446-489
 
 Every call runs through the CUDA library; there is no CPU fallback.  If the
 library has not been built (or cannot be loaded) the import fails.
@@ -37,6 +40,7 @@ MAX_K = 8
 SEQ_EDGE_STREAMS = 1
 SEQ_WAVES = 2
 TRIM_EXACT, TRIM_FAST = 0, 1
+SAMPLE_TARGET = 10_000_000  # the reference's CLIQUES_TO_SAMPLE
 GEN_CHUNG_LU, GEN_RMAT, GEN_ER, GEN_PLANTED, GEN_RMAT_PLANTED = 1, 2, 3, 4, 5
 
 
@@ -73,6 +77,21 @@ class StateInfo(C.Structure):
 class ExactInfo(C.Structure):
     _fields_ = [("num", C.c_uint64), ("den", C.c_uint64), ("density", C.c_double), ("size", C.c_uint32),
                 ("cliques", C.c_uint64), ("cliques_total", C.c_uint64), ("iterations", C.c_int)]
+
+
+class SamplingInfo(C.Structure):
+    _fields_ = [("cliques_total", C.c_uint64), ("sampled", C.c_uint64), ("prob", C.c_double),
+                ("threshold", C.c_uint64), ("all", C.c_int), ("waves", C.c_uint32), ("passes", C.c_uint32)]
+
+
+class SamplingReport(C.Structure):
+    _fields_ = [("T", C.c_uint32), ("n", C.c_uint32), ("m", C.c_uint64), ("density", C.c_double),
+                ("ub", C.c_double), ("sub_n", C.c_uint32), ("sub_e", C.c_uint64), ("sub_core", C.c_uint32),
+                ("sub_cliques", C.c_uint64), ("edge_density", C.c_double), ("clique_density", C.c_double),
+                ("upper_bound", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class KernelTime(C.Structure):
@@ -209,6 +228,16 @@ _SIGS = {
     "kclpp_trim_copy": (C.c_int, [_P, _u32p, _u64p, _u32p, _u64p]),
     "kclpp_trim_edges": (C.c_int, [_P, C.POINTER(_P)]),
     "kclpp_trim_free": (None, [_P]),
+    "kclpp_sampling_create": (C.c_int, [_P, _P, C.c_int, C.c_uint64, C.c_uint64, C.c_uint32, C.POINTER(_P)]),
+    "kclpp_sampling_info_get": (C.c_int, [_P, C.POINTER(SamplingInfo)]),
+    "kclpp_sampling_cliques": (C.c_int, [_P, _P, _u32p, C.POINTER(C.c_uint8)]),
+    "kclpp_sampling_passes": (C.c_int, [_P, _P, C.c_uint32]),
+    "kclpp_sampling_get_rho": (C.c_int, [_P, _P, _u32p]),
+    "kclpp_sampling_set_rho": (C.c_int, [_P, _P, _u32p, C.c_uint32]),
+    "kclpp_sampling_extract": (C.c_int, [_P, _P, C.c_uint32, C.POINTER(SamplingReport), _u32p]),
+    "kclpp_sampling_free": (None, [_P]),
+    "kclpp_sampling_main": (C.c_int, [_P, _P, C.c_int, C.c_uint32, C.c_uint64, C.c_uint64, C.c_uint32,
+                                      C.POINTER(SamplingReport), C.c_int, C.POINTER(C.c_int)]),
 }
 for _name, (_res, _args) in _SIGS.items():
     _f = getattr(_lib, _name)
@@ -710,3 +739,67 @@ def densest_exact(el: EdgeList, k: int) -> tuple[ExactInfo, np.ndarray]:
     mask = np.zeros(max(el.n, 1), dtype=np.uint8)
     _check(_lib.kclpp_densest_exact(el._h, k, C.byref(info), mask.ctypes.data_as(_P)))
     return info, mask[: el.n].astype(bool)
+
+
+class Sampling:
+    """Seq-Sampling++ (kCDensestSamplingKclistpp.c): a sample of the graph's
+    k-cliques kept on the device, "++" passes over it, and reports.  The graph
+    must stay open while the sampling object is in use."""
+
+    def __init__(self, g: Graph, k: int, target: int = SAMPLE_TARGET, seed: int = 1, waves: int = 8):
+        self.g, self.k = g, k
+        self._h = _P()
+        _check(_lib.kclpp_sampling_create(g.ctx.handle, g._h, k, target, seed, waves, C.byref(self._h)))
+
+    def info(self) -> SamplingInfo:
+        i = SamplingInfo()
+        _check(_lib.kclpp_sampling_info_get(self._h, C.byref(i)))
+        return i
+
+    def cliques(self) -> tuple[np.ndarray, np.ndarray]:
+        """Kept cliques as (rows (S, k) of ascending ids, lexicographic by the
+        largest member first; each row's wave)."""
+        S = self.info().sampled
+        rows = np.zeros((max(S, 1), self.k), dtype=np.uint32)
+        wave = np.zeros(max(S, 1), dtype=np.uint8)
+        _check(_lib.kclpp_sampling_cliques(self.g.ctx.handle, self._h, _ptr(rows, C.c_uint32),
+                                           _ptr(wave, C.c_uint8)))
+        return rows[:S], wave[:S]
+
+    def passes(self, count: int) -> None:
+        _check(_lib.kclpp_sampling_passes(self.g.ctx.handle, self._h, count))
+
+    def rho(self) -> np.ndarray:
+        r = np.zeros(max(self.g.n, 1), dtype=np.uint32)
+        _check(_lib.kclpp_sampling_get_rho(self.g.ctx.handle, self._h, _ptr(r, C.c_uint32)))
+        return r[: self.g.n]
+
+    def set_rho(self, rho: np.ndarray, passes: int) -> None:
+        r = np.ascontiguousarray(rho, dtype=np.uint32)
+        _check(_lib.kclpp_sampling_set_rho(self.g.ctx.handle, self._h, _ptr(r, C.c_uint32), passes))
+
+    def extract(self, T: int) -> tuple[SamplingReport, np.ndarray]:
+        """Report for loads that stand for T passes, and the vertices by decreasing load."""
+        rep = SamplingReport()
+        order = np.zeros(max(self.g.n, 1), dtype=np.uint32)
+        _check(_lib.kclpp_sampling_extract(self.g.ctx.handle, self._h, T, C.byref(rep), _ptr(order, C.c_uint32)))
+        return rep, order[: self.g.n]
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            _lib.kclpp_sampling_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        self.close()
+
+
+def sampling_main(g: Graph, k: int, num_iter: int, target: int = SAMPLE_TARGET, seed: int = 1,
+                  waves: int = 8) -> list[SamplingReport]:
+    """Solve: sample, then one report per power of two up to num_iter passes."""
+    cap = max(1, num_iter.bit_length())
+    reps = (SamplingReport * cap)()
+    cnt = C.c_int()
+    _check(_lib.kclpp_sampling_main(g.ctx.handle, g._h, k, num_iter, target, seed, waves, reps, cap,
+                                    C.byref(cnt)))
+    return [reps[i] for i in range(cnt.value)]

@@ -51,6 +51,11 @@ cudaStream_t ctx_stream(kclpp_ctx *c);
 int ctx_device(kclpp_ctx *c);
 int ctx_sms(kclpp_ctx *c);
 void ctx_count_launch(kclpp_ctx *c, int n);
+// Graph accessors for the same: the host DAG and its device copy.
+const HostDag &graph_dag(const kclpp_graph *g);
+const uint64_t *graph_dev_offsets(const kclpp_graph *g);
+const uint32_t *graph_dev_cols(const kclpp_graph *g);
+int graph_device(const kclpp_graph *g);
 
 // SortByCore with the reference heap's tie order.
 void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank);

@@ -1067,3 +1067,193 @@ void orc_free_trim(orc_trim_result *r) {
   free(r->map); free(r->nck); free(r->order); free(r->core_num); free(r->trimmed);
   memset(r, 0, sizeof *r);
 }
+
+/* ======================================================================== */
+/* Seq-Sampling++ (kCDensestSamplingKclistpp.c) with the library's
+ * counter-based sample in place of rand(): a clique Q is kept iff
+ * mix64(sum of key(v), v in Q) < threshold (or every clique with all), key(v)
+ * = mix64(seed + (v + 1) * 0x9E3779B97F4A7C15), mix64 = SplitMix64's output
+ * function (Steele, Lea and Flood, OOPSLA 2014); its wave is
+ * ((mix64(sum ^ 0xD1B54A32D192ED03) >> 32) * waves) >> 32.                  */
+static inline uint64_t smp_mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+uint64_t orc_sample_key(uint64_t seed, uint32_t v) {
+  return smp_mix64(seed + ((uint64_t)v + 1ull) * 0x9E3779B97F4A7C15ull);
+}
+
+typedef struct {
+  uint64_t seed, threshold;
+  int all;
+  uint32_t waves;
+  uint32_t *rows;
+  uint8_t *wave;
+  uint64_t cap, kept;
+  uint32_t pre[ORC_MAXK];  /* global ids of the prefix: s, t, then deeper members */
+} sample_t;
+
+/* One clique: the prefix pre[0, depth) plus the members in last[0, nl)
+ * (deepest last). */
+static void sample_one(sample_t *st, int k, int depth, const uint32_t *last, int nl) {
+  uint64_t h = 0;
+  for (int q = 0; q < depth; ++q) h += orc_sample_key(st->seed, st->pre[q]);
+  for (int q = 0; q < nl; ++q) h += orc_sample_key(st->seed, last[q]);
+  if (!st->all && !(smp_mix64(h) < st->threshold)) return;
+  if (st->kept < st->cap) {
+    /* ascending ids: deepest member first (the ck[] rows,
+     * kCDensestSamplingKclistpp.c:166-170 and 204-209) */
+    uint32_t *row = st->rows + st->kept * (uint64_t)k;
+    int j = 0;
+    for (int q = nl - 1; q >= 0; --q) row[j++] = last[q];
+    for (int q = depth - 1; q >= 0; --q) row[j++] = st->pre[q];
+    st->wave[st->kept] = (uint8_t)(((smp_mix64(h ^ 0xD1B54A32D192ED03ull) >> 32) * (uint64_t)st->waves) >> 32);
+  }
+  st->kept++;
+}
+
+/* KCLIST_CliqueEnumThread with the SAMPLING task
+ * (kCDensestSamplingKclistpp.c:148-258), on the workspace of the other
+ * passes: every clique in enumeration order.                              */
+static void sample_rec(orc_ws *w, sample_t *st, int l, int depth) {
+  if (w->k == 3) {
+    for (uint32_t i = 0; i < w->nn[1]; ++i) {
+      uint32_t x = w->sg2g[w->nodes[1][i]];
+      sample_one(st, 3, depth, &x, 1);
+    }
+    return;
+  }
+  if (l == 2) {
+    for (uint32_t i = 0; i < w->nn[2]; ++i) {
+      uint32_t u = w->nodes[2][i];
+      const uint32_t *au = w->adj[2] + (size_t)w->core * u;
+      for (uint32_t j = 0; j < w->deg[2][u]; ++j) {
+        uint32_t last[2] = {w->sg2g[u], w->sg2g[au[j]]};
+        sample_one(st, w->k, depth, last, 2);
+      }
+    }
+    return;
+  }
+  if (w->nn[l] < (uint32_t)l) return;
+  for (uint32_t i = 0; i < w->nn[l]; ++i) {
+    uint32_t u = w->nodes[l][i];
+    st->pre[depth] = w->sg2g[u];
+    descend(w, l, u);
+    sample_rec(w, st, l - 1, depth + 1);
+    ascend(w, l);
+  }
+}
+
+uint64_t orc_sampling_collect(const orc_graph *g, int k, uint64_t seed, uint64_t threshold, int all,
+                              uint32_t waves, uint32_t *rows, uint8_t *wave, uint64_t cap) {
+  if (k < 3 || k > ORC_MAXK || g->e == 0) return 0;
+  sample_t st;
+  memset(&st, 0, sizeof st);
+  st.seed = seed;
+  st.threshold = threshold;
+  st.all = all;
+  st.waves = waves;
+  st.rows = rows;
+  st.wave = wave;
+  st.cap = cap;
+  orc_ws *w = ws_new(g, k);
+  for (uint64_t i = 0; i < g->e; ++i) {  /* root edges in (s, t) order, :287-292 */
+    st.pre[0] = g->edges[i].s;
+    st.pre[1] = g->edges[i].t;
+    make_subgraph(w, g, g->edges[i].s, g->edges[i].t);
+    sample_rec(w, &st, k - 2, 2);
+  }
+  ws_free(w);
+  return st.kept;
+}
+
+/* The member of a stored clique that takes its unit: the smallest value,
+ * ties to the earliest member of the row (InMemoryFrankWolfe,
+ * kCDensestSamplingKclistpp.c:353-359). */
+static inline uint32_t smp_argmin(const uint32_t *row, int k, const uint32_t *rho) {
+  uint32_t g = row[0];
+  for (int j = 1; j < k; ++j)
+    if (rho[row[j]] < rho[g]) g = row[j];
+  return g;
+}
+
+/* InMemoryFrankWolfe's update (:345-361) with the visiting order given:
+ * order[q] is the row taken at step q. */
+void orc_sampling_pass_order(int k, uint64_t S, const uint32_t *rows, const uint32_t *order, uint32_t *rho) {
+  for (uint64_t q = 0; q < S; ++q) ++rho[smp_argmin(rows + (uint64_t)order[q] * k, k, rho)];
+}
+
+/* The library's wave pass: waves one after another; the rows of a wave all
+ * read the values the earlier waves left. */
+void orc_sampling_pass(uint32_t n, int k, uint64_t S, const uint32_t *rows, const uint8_t *wave, uint32_t waves,
+                       uint32_t *rho) {
+  uint32_t *delta = (uint32_t *)xcalloc((size_t)n + 1, sizeof(uint32_t));
+  for (uint32_t w = 0; w < waves; ++w) {
+    for (uint64_t i = 0; i < S; ++i)
+      if (wave[i] == w) ++delta[smp_argmin(rows + i * (uint64_t)k, k, rho)];
+    for (uint32_t v = 0; v < n; ++v) {
+      rho[v] += delta[v];
+      delta[v] = 0;
+    }
+  }
+  free(delta);
+}
+
+static const uint32_t *smp_sort_rho;
+static int smp_rho_desc(const void *a, const void *b) {
+  uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+  if (smp_sort_rho[x] != smp_sort_rho[y]) return smp_sort_rho[x] > smp_sort_rho[y] ? -1 : 1;
+  return x < y ? -1 : (x > y);
+}
+
+/* ExtractDensest (kCDensestSamplingKclistpp.c:364-419): vertices by
+ * decreasing load (ties: ascending id), each stored clique to its last vertex
+ * in that order, the first strictly densest prefix, and the bound from the
+ * loads.  Counters are 64-bit where the reference's unsigned would wrap. */
+orc_sampling_info orc_sampling_extract(uint32_t n, int k, uint64_t S, const uint32_t *rows, const uint32_t *rho,
+                                       uint32_t T, uint32_t *ordered) {
+  orc_sampling_info info;
+  memset(&info, 0, sizeof info);
+  if (n == 0) return info;
+  uint32_t *rank = (uint32_t *)xmalloc((size_t)n * sizeof(uint32_t));
+  uint64_t *push = (uint64_t *)xcalloc(n, sizeof(uint64_t));
+  for (uint32_t i = 0; i < n; ++i) ordered[i] = i;
+  smp_sort_rho = rho;
+  qsort(ordered, n, sizeof(uint32_t), smp_rho_desc);
+  for (uint32_t i = 0; i < n; ++i) rank[ordered[i]] = i;
+  for (uint64_t i = 0; i < S; ++i) {
+    const uint32_t *row = rows + i * (uint64_t)k;
+    uint32_t top = row[0];
+    for (int j = 1; j < k; ++j)
+      if (rank[row[j]] > rank[top]) top = row[j];
+    ++push[rank[top]];
+  }
+  info.density = -1;
+  uint64_t cnt = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    cnt += push[i];
+    if (info.density < (double)cnt / (i + 1)) {
+      info.n = i + 1;
+      info.m = cnt;
+      info.density = (double)cnt / (i + 1);
+    }
+  }
+  uint64_t sum = 0;
+  double ip1ck = 0;
+  info.ub = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    sum += rho[ordered[i]];
+    if (i + 1 == (uint32_t)k) ip1ck = 1;
+    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
+    if (ip1ck < (double)sum / T) {
+      info.ub = ip1ck / (i + 1);
+    } else {
+      if (info.ub < (double)sum / T / (i + 1)) info.ub = (double)sum / T / (i + 1);
+      break;
+    }
+  }
+  free(rank);
+  free(push);
+  return info;
+}

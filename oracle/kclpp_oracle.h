@@ -114,6 +114,28 @@ typedef struct {
 int orc_trim(uint32_t n, uint64_t e, const orc_edge *edges, int k, orc_trim_result *out);
 void orc_free_trim(orc_trim_result *r);
 
+/* ---- Seq-Sampling++ (kCDensestSamplingKclistpp.c), with the library's
+ * counter-based sample in place of rand() ---------------------------------- */
+typedef struct {
+  uint32_t n;       /* densest prefix by the stored cliques (info.n) */
+  uint64_t m;       /* stored cliques pushed inside it (info.m)      */
+  double density;
+  double ub;
+} orc_sampling_info;
+uint64_t orc_sample_key(uint64_t seed, uint32_t v);
+/* Every k-clique in enumeration order; the kept ones go to rows (ascending
+ * ids, up to cap rows) with their wave.  Returns the number kept. */
+uint64_t orc_sampling_collect(const orc_graph *g, int k, uint64_t seed, uint64_t threshold, int all,
+                              uint32_t waves, uint32_t *rows, uint8_t *wave, uint64_t cap);
+/* InMemoryFrankWolfe's update with a given visiting order. */
+void orc_sampling_pass_order(int k, uint64_t S, const uint32_t *rows, const uint32_t *order, uint32_t *rho);
+/* The library's wave-ordered pass. */
+void orc_sampling_pass(uint32_t n, int k, uint64_t S, const uint32_t *rows, const uint8_t *wave, uint32_t waves,
+                       uint32_t *rho);
+/* ExtractDensest; ordered gets the n vertices by decreasing load. */
+orc_sampling_info orc_sampling_extract(uint32_t n, int k, uint64_t S, const uint32_t *rows, const uint32_t *rho,
+                                       uint32_t T, uint32_t *ordered);
+
 /* ---- whole-program drivers (CDF_Main) ---------------------------------- */
 /* Runs passes 1..2^floor(log2 num_iter) and writes one orc_info per power of two
  * into infos (capacity max_infos); returns the number of infos written. */

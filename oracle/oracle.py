@@ -45,6 +45,10 @@ class OrcInfo(C.Structure):
         return (self.n, self.m, self.cliques, self.density, self.ub)
 
 
+class OrcSamplingInfo(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("m", C.c_uint64), ("density", C.c_double), ("ub", C.c_double)]
+
+
 class OrcTrim(C.Structure):
     _fields_ = [("n", C.c_uint32), ("e", C.c_uint64), ("n2", C.c_uint32), ("e2", C.c_uint64),
                 ("core", C.c_uint32), ("map", C.POINTER(C.c_uint32)), ("nck", C.POINTER(C.c_uint64)),
@@ -89,6 +93,14 @@ def lib() -> C.CDLL:
             "orc_seq_pass_waves": (C.c_int, [G, C.c_int, u64p, C.c_uint32, C.c_int]),
             "orc_seq_delta_masked": (C.c_int, [G, C.c_int, u64p, C.POINTER(C.c_uint8), C.c_int, u64p]),
             "orc_sim_counts_masked": (None, [G, C.c_int, f64p, C.POINTER(C.c_uint8), C.c_int, u64p]),
+            "orc_sample_key": (C.c_uint64, [C.c_uint64, C.c_uint32]),
+            "orc_sampling_collect": (C.c_uint64, [G, C.c_int, C.c_uint64, C.c_uint64, C.c_int, C.c_uint32, u32p,
+                                                  C.POINTER(C.c_uint8), C.c_uint64]),
+            "orc_sampling_pass_order": (None, [C.c_int, C.c_uint64, u32p, u32p, u32p]),
+            "orc_sampling_pass": (None, [C.c_uint32, C.c_int, C.c_uint64, u32p, C.POINTER(C.c_uint8), C.c_uint32,
+                                         u32p]),
+            "orc_sampling_extract": (OrcSamplingInfo, [C.c_uint32, C.c_int, C.c_uint64, u32p, u32p, C.c_uint32,
+                                                       u32p]),
             "orc_wtime": (C.c_double, []),
             "orc_max_threads": (C.c_int, []),
         }
@@ -247,6 +259,19 @@ class Graph:
             raise ValueError("oracle seq_main: unsupported k")
         return [infos[i] for i in range(min(c, cap))], r[: self.n]
 
+    # ---- Seq-Sampling++ ----
+    def sampling_collect(self, k: int, seed: int, threshold: int, all_: bool, waves: int):
+        """Kept cliques in enumeration order: rows (S, k) of ascending ids, waves (S,)."""
+        L = lib()
+        kept = int(L.orc_sampling_collect(self._g, k, seed, threshold, int(all_), waves,
+                                          C.POINTER(C.c_uint32)(), C.POINTER(C.c_uint8)(), 0))
+        rows = np.zeros((max(kept, 1), k), dtype=np.uint32)
+        wave = np.zeros(max(kept, 1), dtype=np.uint8)
+        got = int(L.orc_sampling_collect(self._g, k, seed, threshold, int(all_), waves, _p(rows, C.c_uint32),
+                                         _p(wave, C.c_uint8), kept))
+        assert got == kept
+        return rows[:kept], wave[:kept]
+
     def sim_main(self, k: int, num_iter: int, threads: int = 1):
         cap = 40
         infos = (OrcInfo * cap)()
@@ -301,3 +326,89 @@ def wtime() -> float:
 
 def max_threads() -> int:
     return lib().orc_max_threads()
+
+
+# ---- Seq-Sampling++ (kCDensestSamplingKclistpp.c) ----------------------------
+def sampling_key(seed: int, v: int) -> int:
+    return int(lib().orc_sample_key(seed, v))
+
+
+def sampling_threshold(target: int, total: int):
+    """(all, prob, threshold) as the library derives them from p = target / total
+    (kCDensestSamplingKclistpp.c:272)."""
+    import math
+    if target >= total:
+        return True, 1.0, 0
+    prob = target / total
+    return False, prob, int(math.ldexp(prob, 64))
+
+
+def sampling_pass(n: int, k: int, rows: np.ndarray, wave: np.ndarray, waves: int, rho: np.ndarray) -> np.ndarray:
+    rows = np.ascontiguousarray(rows, dtype=np.uint32)
+    wave = np.ascontiguousarray(wave, dtype=np.uint8)
+    rho = np.array(rho, dtype=np.uint32, copy=True)
+    rho = np.concatenate([rho, np.zeros(1, np.uint32)])
+    lib().orc_sampling_pass(n, k, len(wave), _p(rows, C.c_uint32), _p(wave, C.c_uint8), waves, _p(rho, C.c_uint32))
+    return rho[:n]
+
+
+def sampling_pass_order(k: int, rows: np.ndarray, order: np.ndarray, rho: np.ndarray) -> np.ndarray:
+    rows = np.ascontiguousarray(rows, dtype=np.uint32)
+    order = np.ascontiguousarray(order, dtype=np.uint32)
+    rho = np.array(rho, dtype=np.uint32, copy=True)
+    lib().orc_sampling_pass_order(k, len(order), _p(rows, C.c_uint32), _p(order, C.c_uint32), _p(rho, C.c_uint32))
+    return rho
+
+
+def sampling_extract(n: int, k: int, rows: np.ndarray, rho: np.ndarray, T: int):
+    rows = np.ascontiguousarray(rows, dtype=np.uint32)
+    rho = np.ascontiguousarray(rho, dtype=np.uint32)
+    ordered = np.zeros(max(n, 1), dtype=np.uint32)
+    info = lib().orc_sampling_extract(n, k, rows.shape[0], _p(rows, C.c_uint32), _p(rho, C.c_uint32), T,
+                                      _p(ordered, C.c_uint32))
+    return info, ordered[:n]
+
+
+def sampling_report(g: Graph, k: int, rows: np.ndarray, rho: np.ndarray, T: int, prob: float) -> dict:
+    """One report line of Solve (kCDensestSamplingKclistpp.c:460-478): the
+    densest prefix of the loads, the exact count in its induced subgraph
+    (MakeDensestSubgraphEdgeList, :420-435, then SortByCore, Relabel, MakeGraph
+    and the COUNT_IN_SUBGRAPH task) and the figures of the printed line."""
+    import math
+    info, ordered = sampling_extract(g.n, k, rows, rho, T)
+    rank = np.empty(g.n, dtype=np.int64)
+    rank[ordered] = np.arange(g.n)
+    E = g.edges().astype(np.int64)
+    keep = (rank[E[:, 0]] < info.n) & (rank[E[:, 1]] < info.n) if len(E) else np.zeros(0, bool)
+    sub = np.stack([rank[E[keep, 0]], rank[E[keep, 1]]], axis=1).astype(np.uint32) if keep.any() else None
+    if sub is None:
+        sub_n, sub_e, sub_core, cliques = 0, 0, 0, 0
+    else:
+        sg = Graph(sub, n=info.n)
+        sub_n, sub_e, sub_core = sg.n, sg.m, sg.core
+        cliques = sg.count_cliques(k)[0]
+    with np.errstate(all="ignore"):
+        edge_density = float(np.float64(sub_e) * 2.0 / np.float64(sub_n) / np.float64((sub_n - 1) & 0xFFFFFFFF))
+        clique_density = float(np.float64(cliques) / np.float64(sub_n))
+        ub = np.float64(info.ub)
+        upper = float(ub / np.float64(prob) / (1 - np.sqrt(6 * np.float64(math.log(g.n)) / ub)))
+    return {"T": T, "n": info.n, "m": info.m, "density": info.density, "ub": info.ub, "sub_n": sub_n,
+            "sub_e": sub_e, "sub_core": sub_core, "sub_cliques": cliques, "edge_density": edge_density,
+            "clique_density": clique_density, "upper_bound": upper, "order": ordered}
+
+
+def sampling_main(g: Graph, k: int, num_iter: int, target: int, seed: int, waves: int):
+    """Solve (:446-489) with the library's sample and wave passes: one report per power of two."""
+    total = g.count_cliques(k)[0]
+    all_, prob, thr = sampling_threshold(target, total)
+    rows, wave = g.sampling_collect(k, seed, thr, all_, waves)
+    rho = np.zeros(g.n, dtype=np.uint32)
+    reps, done, T = [], 0, 1
+    while T <= num_iter:
+        for _ in range(T - done):
+            rho = sampling_pass(g.n, k, rows, wave, waves, rho)
+        done = T
+        reps.append(sampling_report(g, k, rows, rho, T, prob))
+        T <<= 1
+    return {"total": total, "prob": prob, "threshold": thr, "all": all_, "rows": rows, "wave": wave,
+            "rho": rho, "reports": reps}

@@ -1,9 +1,12 @@
 """The CPU oracle against the golden vectors produced by the reference itself.
 
 This pins the oracle: every number below was printed by the reference's own
-functions (kCDensestNoAtom.c, kCDensestCmpSync.c, kClistCoreTrim.c compiled
-from source), and the oracle must reproduce it bit for bit.
+functions (kCDensestNoAtom.c, kCDensestCmpSync.c, kClistCoreTrim.c,
+kCDensestSamplingKclistpp.c compiled from source), and the oracle must
+reproduce it bit for bit.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -121,3 +124,41 @@ def test_sim_k2_matches_reference():
         want = [[i[0], i[1], i[2], float.fromhex(i[3]), float.fromhex(i[4])] for i in meta["infos"]]
         assert G.infos_equal(want, infos), name
         assert np.array_equal(rho.view(np.uint64), arrays[f"{name}_rho_bits"]), name
+
+
+def _sampling_cases():
+    import json
+    import os
+
+    with open(os.path.join(G.HERE, "sampling.json")) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("key", sorted(_sampling_cases()))
+def test_sampling_matches_reference(key):
+    """Seq-Sampling++ (kCDensestSamplingKclistpp.c): the reference's clique
+    list at p = 1, its InMemoryFrankWolfe update in the order its own shuffle
+    drew, ExtractDensest bit for bit, and Solve's printed report line -- all
+    reproduced by the oracle from the stored order (tests/golden/
+    make_golden_sampling.py)."""
+    from tests.golden.make_golden_sampling import check_line, rows_digest
+
+    meta = _sampling_cases()[key]
+    k = meta["k"]
+    with np.load(os.path.join(G.HERE, "sampling.npz")) as z:
+        order, rho_ref = z[f"{key}_order"], z[f"{key}_rho"]
+    g = O.Graph(G.pairs(meta["case"]))
+    total = g.count_cliques(k)[0]
+    assert total == meta["total"]
+    full, _ = g.sampling_collect(k, meta["sample_seed"], 0, True, meta["waves"])
+    assert rows_digest(full) == meta["all_digest"]
+    all_, prob, thr = O.sampling_threshold(meta["target"], total)
+    assert prob.hex() == meta["prob"]
+    rows, _ = g.sampling_collect(k, meta["sample_seed"], thr, all_, meta["waves"])
+    assert len(rows) == meta["sampled"]
+    rho = O.sampling_pass_order(k, rows, order, np.zeros(g.n, np.uint32))
+    assert np.array_equal(rho, rho_ref)
+    info, _ = O.sampling_extract(g.n, k, rows, rho, 1)
+    want = meta["info"]
+    assert [info.n, info.m, info.density.hex(), info.ub.hex()] == want
+    check_line(O.sampling_report(g, k, rows, rho, 1, prob), meta["line"])
