@@ -12,8 +12,9 @@
  *    thread-local message for the last failure.  No exception crosses the ABI.
  *  - Host buffers are caller-owned.  Device buffers (the *_dev entry points)
  *    are caller-owned device pointers on the context's device.  Handles
- *    (kclpp_ctx, kclpp_edge_list, kclpp_graph, kclpp_trim_result) are owned by
- *    the library and released with their *_free / kclpp_destroy call.
+ *    (kclpp_ctx, kclpp_edge_list, kclpp_graph, kclpp_trim_result,
+ *    kclpp_batch, kclpp_warm_model, kclpp_sampling) are owned by the library
+ *    and released with their *_free / kclpp_destroy call.
  *  - A context owns one CUDA stream (the caller's, if one is given) and is
  *    meant for one host thread at a time.
  *  - Graphs must be simple: no self loops and no repeated edges (the
