@@ -541,7 +541,6 @@ kclpp_status kclpp_sampling_extract(kclpp_ctx *c, kclpp_sampling *s, uint32_t T,
   // their position in the order, through the library's own pipeline.
   const HostDag &D = graph_dag(s->g);
   std::vector<uint32_t> pairs;
-  std::vector<uint8_t> touched(rep->n, 0);
   for (uint32_t a = 0; a < D.n; ++a) {
     if (rank[a] >= rep->n) continue;
     for (uint64_t e = D.off[a]; e < D.off[a + 1]; ++e) {
@@ -549,7 +548,6 @@ kclpp_status kclpp_sampling_extract(kclpp_ctx *c, kclpp_sampling *s, uint32_t T,
       if (rank[b] >= rep->n) continue;
       pairs.push_back(rank[a]);
       pairs.push_back(rank[b]);
-      touched[rank[a]] = touched[rank[b]] = 1;
     }
   }
   rep->sub_e = pairs.size() / 2;
