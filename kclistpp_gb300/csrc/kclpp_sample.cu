@@ -213,7 +213,13 @@ kclpp_status launch_groups(kclpp_ctx *c, kclpp_sampling *S, const SampleArgs &ba
   uint32_t b2 = b1;
   while (b2 < nr && deg(roots_by_degree[b2]) > kSmallRoots) ++b2;
   const uint32_t bounds[4] = {0, b1, b2, nr};
-  uint32_t *slab = nullptr;
+  // The slab is freed on every return path (cudaFree waits for the kernels).
+  struct Slab {
+    uint32_t *p = nullptr;
+    ~Slab() {
+      if (p) cudaFree(p);
+    }
+  } slab;
   for (int grp = 0; grp < 3; ++grp) {
     const uint32_t lo = bounds[grp], hi = bounds[grp + 1];
     if (lo == hi) continue;
@@ -231,19 +237,15 @@ kclpp_status launch_groups(kclpp_ctx *c, kclpp_sampling *S, const SampleArgs &ba
     const uint32_t grid = std::min<uint32_t>((uint32_t)per_sm * (uint32_t)sms, a.num_roots);
     if (!in_smem) {
       a.slab_words = (uint64_t)a.dmax * a.ws;
-      SCUDA(dalloc(&slab, (size_t)grid * a.slab_words));
-      a.slab = slab;
+      SCUDA(dalloc(&slab.p, (size_t)grid * a.slab_words));
+      a.slab = slab.p;
     }
     fn<<<grid, kSampleThreads, smem, st>>>(a);
     cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) {
-      if (slab) cudaFree(slab);
-      return set_error(KCLPP_ERR_CUDA, "sampling kernel: %s", cudaGetErrorString(e));
-    }
+    if (e != cudaSuccess) return set_error(KCLPP_ERR_CUDA, "sampling kernel: %s", cudaGetErrorString(e));
     ctx_count_launch(c, 1);
   }
   cudaError_t e = cudaStreamSynchronize(st);
-  if (slab) cudaFree(slab);
   if (e != cudaSuccess) return set_error(KCLPP_ERR_CUDA, "sampling kernel: %s", cudaGetErrorString(e));
   return KCLPP_OK;
 }
