@@ -28,7 +28,9 @@ sampled during the timed region, and `convergence`: wall time to a certified
 for the zero start, the learned warm start and the wave ordering
 (`--no-convergence` skips it).  `--workload batch` measures the batched
 configuration instead (many uneven graphs x k = 3..7 in one captured CUDA
-graph) and prints its own line.
+graph) and prints its own line; `--workload sampling` times Seq-Sampling++
+(count, 10^7-clique sample, "++" passes over it, one report) on the untrimmed
+RMAT graph of `--scale`.
 """
 from __future__ import annotations
 
@@ -342,6 +344,52 @@ def batch_workload(K, ctx, a) -> dict:
                     "download of the r vectors"}
 
 
+def sampling_workload(K, ctx, a) -> dict:
+    """Seq-Sampling++ (kCDensestSamplingKclistpp.c) on the RMAT graph of
+    --scale (untrimmed, seeded), k = --k: the exact clique count, the sample
+    of 10^7 cliques kept on the device, one "++" pass over the sample per
+    step (8 waves), and one report (densest prefix, exact count of its
+    subgraph, bound)."""
+    t0 = time.perf_counter()
+    el = K.rmat(a.scale, 16, seed=a.seed)
+    g = K.build_graph(ctx, el)
+    prep_s = time.perf_counter() - t0
+    K.count_cliques(g, a.k)  # warm-up
+    t0 = time.perf_counter()
+    total, _ = K.count_cliques(g, a.k)
+    count_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    smp = K.Sampling(g, a.k, K.SAMPLE_TARGET, a.seed, 8)
+    create_s = time.perf_counter() - t0
+    info = smp.info()
+    for _ in range(max(3, a.warmup)):
+        smp.passes(1)
+    times = []
+    for _ in range(max(1, a.steps)):
+        t0 = time.perf_counter()
+        smp.passes(1)
+        times.append(time.perf_counter() - t0)
+    T = smp.info().passes
+    t0 = time.perf_counter()
+    rep, _ = smp.extract(T)
+    extract_s = time.perf_counter() - t0
+    sec = statistics.median(times)
+    out = {"metric": "sampled k-cliques/s (Seq-Sampling++ pass)", "value": info.sampled / sec,
+           "unit": "k-cliques/s", "n_gpus": 1, "steps": len(times), "warmup": max(3, a.warmup),
+           "ms_per_step": 1000 * sec, "higher_is_better": True, "dtype": "u32", "data": "synthetic",
+           "config": {"workload": f"sampling: rmat{a.scale}-ef16 (0.57,0.19,0.19,0.05), untrimmed, k={a.k}, "
+                                  f"target {K.SAMPLE_TARGET} cliques, 8 waves", "n": g.n, "m": g.m,
+                      "core": g.core, "k": a.k},
+           "cliques_total": total, "sampled": info.sampled, "prob": info.prob, "count_ms": 1000 * count_s,
+           "create_ms": 1000 * create_s, "extract_ms": 1000 * extract_s, "prep_s": prep_s,
+           "report": {"T": rep.T, "sub_n": rep.sub_n, "sub_e": rep.sub_e, "sub_cliques": rep.sub_cliques,
+                      "clique_density": rep.clique_density, "upper_bound": rep.upper_bound},
+           "note": "one step = one kclpp_sampling_passes(1) call (8 waves, synchronised); create_ms is the "
+                   "count plus the sampling pass"}
+    smp.close()
+    return out
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -352,9 +400,9 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--modes", default="seq,sim")
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "batch"],
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "batch", "sampling"],
                     help="rmat: the default line (RMAT-20 trimmed core); batch: many uneven graphs x k = 3..7 "
-                         "in one captured CUDA graph")
+                         "in one captured CUDA graph; sampling: Seq-Sampling++ on the untrimmed RMAT graph")
     ap.add_argument("--batch-graphs", type=int, default=512)
     ap.add_argument("--batch-nmax", type=float, default=1e5)
     ap.add_argument("--batch-passes", type=int, default=20)
@@ -368,6 +416,11 @@ def main() -> None:
     ap.add_argument("--cache", default=os.path.join(tempfile.gettempdir(), "kclpp_bench_cache"))
     a = ap.parse_args()
     modes = [m for m in a.modes.split(",") if m]
+    if a.impl == "reference" and a.workload != "rmat":
+        if int(os.environ.get("RANK", "0")) == 0:
+            print(json.dumps({"impl": "reference", "unavailable": f"the reference arm times the default workload "
+                                                                  f"only, not --workload {a.workload}"}), flush=True)
+        return
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -394,9 +447,10 @@ def main() -> None:
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = K.Context(local, stream=stream.cuda_stream)
-    if a.workload == "batch":
+    if a.workload in ("batch", "sampling"):
         if rank == 0:
-            print(json.dumps(batch_workload(K, ctx, a)), flush=True)
+            fn = batch_workload if a.workload == "batch" else sampling_workload
+            print(json.dumps(fn(K, ctx, a)), flush=True)
         ctx.close()
         if dist:
             dist.destroy_process_group()
