@@ -129,6 +129,14 @@ kclpp_status kclpp_make_graph(kclpp_ctx *ctx, const kclpp_edge_list *el, const u
                               kclpp_graph **g);
 /* kclpp_core_order followed by kclpp_make_graph (main, kCDensestNoAtom.c:425-427). */
 kclpp_status kclpp_build_graph(kclpp_ctx *ctx, const kclpp_edge_list *el, kclpp_graph **g);
+/* The order by mode.  EXACT is SortByCore (as above).  FAST is the bin-sort
+ * min-degree peel of Batagelj and Zaversnik, O(n + m): the same core numbers
+ * and degeneracy (the DAG's largest out-degree) and the same clique counts,
+ * but its own tie order, so Seq-kClist++'s r differs from the reference's. */
+#define KCLPP_ORDER_EXACT 0
+#define KCLPP_ORDER_FAST 1
+kclpp_status kclpp_core_order_mode(const kclpp_edge_list *el, int mode, uint32_t *rank_out);
+kclpp_status kclpp_build_graph_mode(kclpp_ctx *ctx, const kclpp_edge_list *el, int mode, kclpp_graph **g);
 /* A DAG given directly as host CSR (out-lists strictly below the source and
  * ascending), e.g. one made by another tool from the same edge list. */
 kclpp_status kclpp_graph_from_csr(kclpp_ctx *ctx, uint32_t n, uint64_t m, const uint64_t *offsets,

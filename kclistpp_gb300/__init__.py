@@ -40,6 +40,7 @@ MAX_K = 8
 SEQ_EDGE_STREAMS = 1
 SEQ_WAVES = 2
 TRIM_EXACT, TRIM_FAST = 0, 1
+ORDER_EXACT, ORDER_FAST = 0, 1
 SAMPLE_TARGET = 10_000_000  # the reference's CLIQUES_TO_SAMPLE
 GEN_CHUNG_LU, GEN_RMAT, GEN_ER, GEN_PLANTED, GEN_RMAT_PLANTED = 1, 2, 3, 4, 5
 
@@ -173,6 +174,8 @@ _SIGS = {
     "kclpp_core_order": (C.c_int, [_P, _u32p]),
     "kclpp_make_graph": (C.c_int, [_P, _P, _u32p, C.POINTER(_P)]),
     "kclpp_build_graph": (C.c_int, [_P, _P, C.POINTER(_P)]),
+    "kclpp_core_order_mode": (C.c_int, [_P, C.c_int, _u32p]),
+    "kclpp_build_graph_mode": (C.c_int, [_P, _P, C.c_int, C.POINTER(_P)]),
     "kclpp_graph_from_csr": (C.c_int, [_P, C.c_uint32, C.c_uint64, _u64p, _u32p, C.POINTER(_P)]),
     "kclpp_graph_info": (C.c_int, [_P, _u32p, _u64p, _u32p]),
     "kclpp_graph_copy_csr": (C.c_int, [_P, _u64p, _u32p]),
@@ -410,9 +413,14 @@ def planted(n: int, avg_degree: float, gamma: float, communities: int, comm_min:
                     comm_min=comm_min, comm_max=comm_max, p_in=p_in, seed=seed)
 
 
-def core_order(el: EdgeList) -> np.ndarray:
+def core_order(el: EdgeList, mode: int = ORDER_EXACT) -> np.ndarray:
+    """rank[v] of every vertex: SortByCore's order (ORDER_EXACT) or the bin-sort
+    peel (ORDER_FAST: same core numbers, other ties)."""
     rank = np.empty(el.n, dtype=np.uint32)
-    _check(_lib.kclpp_core_order(el._h, _ptr(rank, C.c_uint32)))
+    if mode == ORDER_EXACT:
+        _check(_lib.kclpp_core_order(el._h, _ptr(rank, C.c_uint32)))
+    else:
+        _check(_lib.kclpp_core_order_mode(el._h, mode, _ptr(rank, C.c_uint32)))
     return rank
 
 
@@ -441,10 +449,12 @@ class Graph:
         self.close()
 
 
-def build_graph(ctx: Context, el: EdgeList, rank: np.ndarray | None = None) -> Graph:
+def build_graph(ctx: Context, el: EdgeList, rank: np.ndarray | None = None, order: int = ORDER_EXACT) -> Graph:
     h = _P()
-    if rank is None:
+    if rank is None and order == ORDER_EXACT:
         _check(_lib.kclpp_build_graph(ctx.handle, el._h, C.byref(h)))
+    elif rank is None:
+        _check(_lib.kclpp_build_graph_mode(ctx.handle, el._h, order, C.byref(h)))
     else:
         rank = np.ascontiguousarray(rank, dtype=np.uint32)
         _check(_lib.kclpp_make_graph(ctx.handle, el._h, _ptr(rank, C.c_uint32), C.byref(h)))

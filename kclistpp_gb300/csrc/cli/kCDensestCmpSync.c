@@ -7,6 +7,8 @@
  * Writes stat_cmpsync_<tag>_<p>_<T>_<k>.txt with the reference's header and
  * one line per power of two (kCDensestCmpSync.c:386-387, 411) and prints the
  * same progress line on stderr (:410).  p is accepted and ignored.
+ * KCLPP_ORDER=fast in the environment builds the DAG from the bin-sort core
+ * order (same degeneracy and clique counts, other ties) instead of SortByCore.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -45,7 +47,9 @@ int main(int argc, char **argv) {
   printf("Number of nodes = %u\nNumber of edges = %llu\n", n, (unsigned long long)e);
   printf("Building the graph structure\n");
   kclpp_graph *g;
-  CHECK(kclpp_build_graph(ctx, el, &g));
+  const char *order = getenv("KCLPP_ORDER");  /* "fast": the bin-sort peel */
+  CHECK(kclpp_build_graph_mode(ctx, el, order && !strcmp(order, "fast") ? KCLPP_ORDER_FAST : KCLPP_ORDER_EXACT,
+                               &g));
   CHECK(kclpp_graph_info(g, &n, &m, &core));
   printf("Core value (max truncated degree) = %u\n", core);
   printf("Number of nodes (degree > 0) = %u\n", n);

@@ -8,9 +8,12 @@
  * (kCDensestNoAtom.c:393).  p is accepted and ignored (the passes run on the
  * GPU); Seq-kClist++ runs with one stream per root edge, the deterministic
  * ordering of the library.  Times are wall-clock milliseconds.
+ * KCLPP_ORDER=fast in the environment builds the DAG from the bin-sort core
+ * order (same degeneracy and clique counts, other ties) instead of SortByCore.
  */
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 #include <time.h>
 
 #include "kclpp.h"
@@ -51,7 +54,9 @@ int main(int argc, char **argv) {
   printf("Number of nodes = %u\nNumber of edges = %llu\n", n, (unsigned long long)e);
   printf("Building the graph structure\n");
   kclpp_graph *g;
-  CHECK(kclpp_build_graph(ctx, el, &g));
+  const char *order = getenv("KCLPP_ORDER");  /* "fast": the bin-sort peel */
+  CHECK(kclpp_build_graph_mode(ctx, el, order && !strcmp(order, "fast") ? KCLPP_ORDER_FAST : KCLPP_ORDER_EXACT,
+                               &g));
   uint64_t m;
   uint32_t core;
   CHECK(kclpp_graph_info(g, &n, &m, &core));

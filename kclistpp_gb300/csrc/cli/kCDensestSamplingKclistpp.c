@@ -14,10 +14,12 @@
  *   KCLPP_SEED            seed of the sample (default 1)
  *   KCLPP_WAVES           waves per pass, 1..256 (default 8)
  *   KCLPP_SAMPLE_TARGET   cliques to sample (default 10^7, CLIQUES_TO_SAMPLE)
+ *   KCLPP_ORDER=fast      the bin-sort core order instead of SortByCore's
  * Times are wall-clock milliseconds.
  */
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 #include <time.h>
 
 #include "kclpp.h"
@@ -76,7 +78,9 @@ int main(int argc, char **argv) {
 
   printf("Building the graph structure\n");
   kclpp_graph *g;
-  CHECK(kclpp_build_graph(ctx, el, &g));
+  const char *order = getenv("KCLPP_ORDER");  /* "fast": the bin-sort peel */
+  CHECK(kclpp_build_graph_mode(ctx, el, order && !strcmp(order, "fast") ? KCLPP_ORDER_FAST : KCLPP_ORDER_EXACT,
+                               &g));
   uint64_t m;
   uint32_t core;
   CHECK(kclpp_graph_info(g, &n, &m, &core));

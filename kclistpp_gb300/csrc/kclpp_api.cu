@@ -657,9 +657,21 @@ kclpp_status kclpp_make_graph(kclpp_ctx *c, const kclpp_edge_list *el, const uin
 }
 
 kclpp_status kclpp_build_graph(kclpp_ctx *c, const kclpp_edge_list *el, kclpp_graph **out) {
+  return kclpp_build_graph_mode(c, el, KCLPP_ORDER_EXACT, out);
+}
+
+kclpp_status kclpp_core_order_mode(const kclpp_edge_list *el, int mode, uint32_t *rank_out) {
+  if (!el || !rank_out) return set_error(KCLPP_ERR_INVALID, "kclpp_core_order_mode: null argument");
+  if (mode == KCLPP_ORDER_EXACT) core_order_host(el->n, el->pairs, rank_out);
+  else if (mode == KCLPP_ORDER_FAST) core_order_fast_host(el->n, el->pairs, rank_out);
+  else return set_error(KCLPP_ERR_INVALID, "unknown order mode %d", mode);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_build_graph_mode(kclpp_ctx *c, const kclpp_edge_list *el, int mode, kclpp_graph **out) {
   if (!c || !el || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_build_graph: null argument");
   std::vector<uint32_t> rank(el->n);
-  KCL_TRY(kclpp_core_order(el, rank.data()));
+  KCL_TRY(kclpp_core_order_mode(el, mode, rank.data()));
   return kclpp_make_graph(c, el, rank.data(), out);
 }
 

@@ -62,6 +62,8 @@ void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *r
 // The same peel: vertices in pop order and the degree each had when popped
 // (degree_at_pop may be null).
 void core_peel_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *order, uint64_t *degree_at_pop);
+// The same peel by bin sort, O(n + m), with its own tie order (KCLPP_ORDER_FAST).
+void core_order_fast_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank);
 // Relabel + sort + CSR; fails on self loops or repeated edges.
 kclpp_status make_dag_host(const std::vector<uint32_t> &pairs, const uint32_t *rank, HostDag &dag);
 

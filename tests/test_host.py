@@ -113,6 +113,56 @@ def test_core_order_matches_oracle(maker):
     assert np.array_equal(K.core_order(el), O.sort_by_core(el.pairs(), el.n))
 
 
+def _out_degrees(el, rank):
+    """Out-degree of every vertex (by id) in the DAG the rank orients."""
+    P = el.pairs().astype(np.int64)
+    by_rank = np.bincount(np.maximum(rank[P[:, 0]], rank[P[:, 1]]), minlength=el.n)
+    return by_rank[rank]
+
+
+def _core_numbers(el, rank):
+    """Core numbers along a peel: the running maximum of the out-degree (the
+    degree each vertex had when it was peeled) in peel order (rank descending)."""
+    od = _out_degrees(el, rank)
+    order = np.argsort(-rank.astype(np.int64), kind="stable")
+    out = np.empty(el.n, dtype=np.int64)
+    out[order] = np.maximum.accumulate(od[order]) if el.n else od
+    return out
+
+
+@pytest.mark.parametrize("maker", [
+    lambda: K.chung_lu(10000, 20.0, 2.5, seed=1),
+    lambda: K.rmat(13, 16, seed=7),
+    lambda: K.planted(8000, 6.0, 2.1, 3, 50, 150, 0.5, seed=2),
+    lambda: K.EdgeList.from_pairs(G.pairs("kat_clique_tree")),
+    lambda: K.EdgeList.from_pairs(G.pairs("kat_star")),
+    lambda: K.EdgeList.from_pairs([[0, 5], [5, 9]]),
+])
+def test_fast_order_is_a_degeneracy_order(maker):
+    """KCLPP_ORDER_FAST: a permutation whose peel has the exact order's core
+    numbers and degeneracy (the DAG's largest out-degree), with the core
+    numbers also equal to networkx's."""
+    el = maker()
+    fast, exact = K.core_order(el, K.ORDER_FAST), K.core_order(el)
+    assert np.array_equal(np.sort(fast), np.arange(el.n, dtype=np.uint32))
+    assert _out_degrees(el, fast).max() == _out_degrees(el, exact).max()
+    cf = _core_numbers(el, fast)
+    assert np.array_equal(cf, _core_numbers(el, exact))
+    nx = pytest.importorskip("networkx")
+    g = nx.Graph()
+    g.add_nodes_from(range(el.n))
+    g.add_edges_from(el.pairs().tolist())
+    want = nx.core_number(g)
+    assert all(cf[v] == want[v] for v in range(el.n))
+
+
+def test_order_mode_rejects_unknown():
+    el = K.EdgeList.from_pairs([[0, 1]])
+    with pytest.raises(K.KclppError) as e:
+        K.core_order(el, 7)
+    assert e.value.status == K.ERR_INVALID
+
+
 def test_oracle_pins_config1_hash():
     p = G.pairs("config1_chung_lu_1e4")
     assert len(p) == 96552
