@@ -333,3 +333,51 @@ def test_normal_graph_core_trim_cli(tmp_path):
     stat = (tmp_path / "stat_trim_x_2.txt").read_text().split("\n")
     assert stat[0].startswith("[Number of Nodes]")
     assert [int(x) for x in stat[1].split("\t")[:3]] == [meta["ntrim"], meta["mtrim"], meta["ncktrim"]]
+
+
+C_CLIENT = r"""
+#include <stdio.h>
+#include <string.h>
+#include "kclpp.h"
+
+int main(void) {
+  /* K_4 plus a pendant edge */
+  const uint32_t pairs[] = {0, 1, 0, 2, 0, 3, 1, 2, 1, 3, 2, 3, 3, 4};
+  kclpp_edge_list *el = NULL;
+  uint32_t n = 0, exact[5], fast[5];
+  uint64_t e = 0;
+  if (kclpp_edge_list_create(pairs, 7, &el) != KCLPP_OK) return 1;
+  if (kclpp_edge_list_info(el, &n, &e) != KCLPP_OK || n != 5 || e != 7) return 2;
+  if (kclpp_core_order(el, exact) != KCLPP_OK) return 3;
+  if (kclpp_core_order_mode(el, KCLPP_ORDER_FAST, fast) != KCLPP_OK) return 4;
+  if (kclpp_core_order_mode(el, 9, fast) != KCLPP_ERR_INVALID) return 5;
+  kclpp_exact_info info;
+  if (kclpp_densest_exact(el, 4, &info, NULL) != KCLPP_OK || info.num != 1 || info.den != 4) return 6;
+  kclpp_sampling *s = NULL;
+  if (kclpp_sampling_create(NULL, NULL, 4, 10, 1, 1, &s) != KCLPP_ERR_INVALID || s) return 7;
+  if (kclpp_sampling_info_get(NULL, NULL) != KCLPP_ERR_INVALID) return 8;
+  printf("%u %u %u %u %u\n", exact[0], exact[1], exact[2], exact[3], exact[4]);
+  kclpp_edge_list_free(el);
+  return strlen(kclpp_version()) ? 0 : 9;
+}
+"""
+
+
+def test_c_client_compiles_links_and_runs(tmp_path):
+    """The header is plain C (C99, -pedantic -Werror) and a C program links
+    the library and calls its host-only entry points."""
+    import shutil
+
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    src = tmp_path / "client.c"
+    src.write_text(C_CLIENT)
+    exe = tmp_path / "client"
+    libdir = os.path.dirname(K.LIB_PATH)
+    subprocess.run(["gcc", "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", libdir, "-lkclpp", "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    rank = [int(x) for x in r.stdout.split()]
+    el = K.EdgeList.from_pairs([[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3], [3, 4]])
+    assert rank == K.core_order(el).tolist()
