@@ -192,6 +192,13 @@ typedef struct {
   int candidates;
 } kclpp_tune_result;
 kclpp_status kclpp_autotune(kclpp_ctx *ctx, kclpp_graph *g, int k, int kernel, kclpp_tune_result *out);
+/* Schedule cache (no reference counterpart): a tuned schedule stored with the
+ * input's kclpp_edge_list_hash, k and kernel, so that later runs skip the
+ * autotuner.  Host only.  Loading checks the file (magic, size, checksum:
+ * KCLPP_ERR_IO) and the key (KCLPP_ERR_INVALID for another graph, k or
+ * kernel); kclpp_graph_set_schedule validates the values. */
+kclpp_status kclpp_schedule_save(const char *path, uint64_t graph_hash, int k, int kernel, const kclpp_schedule *sp);
+kclpp_status kclpp_schedule_load(const char *path, uint64_t graph_hash, int k, int kernel, kclpp_schedule *sp);
 
 /* ---- batches (no reference counterpart) ----------------------------------
  * Many graphs of uneven size as one disjoint union on the device (each graph

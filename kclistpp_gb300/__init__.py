@@ -185,6 +185,8 @@ _SIGS = {
     "kclpp_graph_get_schedule": (C.c_int, [_P, C.POINTER(Schedule)]),
     "kclpp_graph_set_schedule": (C.c_int, [_P, _P, C.POINTER(Schedule)]),
     "kclpp_autotune": (C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
+    "kclpp_schedule_save": (C.c_int, [C.c_char_p, C.c_uint64, C.c_int, C.c_int, C.POINTER(Schedule)]),
+    "kclpp_schedule_load": (C.c_int, [C.c_char_p, C.c_uint64, C.c_int, C.c_int, C.POINTER(Schedule)]),
     "kclpp_batch_create": (C.c_int, [_P, C.POINTER(_P), C.c_uint32, C.POINTER(_P)]),
     "kclpp_batch_info": (C.c_int, [_P, _u32p, _u32p, _u64p, C.POINTER(_P)]),
     "kclpp_batch_vertex_offsets": (C.c_int, [_P, _u32p]),
@@ -478,6 +480,18 @@ def get_schedule(g: Graph) -> Schedule:
 
 def set_schedule(g: Graph, sp: Schedule) -> None:
     _check(_lib.kclpp_graph_set_schedule(g.ctx.handle, g._h, C.byref(sp)))
+
+
+def save_schedule(path: str, graph_hash: int, k: int, kernel: int, sp: Schedule) -> None:
+    """Store a tuned schedule for the graph of that edge-list hash, k and kernel."""
+    _check(_lib.kclpp_schedule_save(os.fsencode(path), graph_hash, k, kernel, C.byref(sp)))
+
+
+def load_schedule(path: str, graph_hash: int, k: int, kernel: int) -> Schedule:
+    """A stored schedule; raises if the file is damaged or was tuned for another key."""
+    sp = Schedule()
+    _check(_lib.kclpp_schedule_load(os.fsencode(path), graph_hash, k, kernel, C.byref(sp)))
+    return sp
 
 
 def autotune(g: Graph, k: int, kernel: int = KERNEL_SEQ) -> TuneResult:

@@ -8,7 +8,9 @@
  * one line per power of two (kCDensestCmpSync.c:386-387, 411) and prints the
  * same progress line on stderr (:410).  p is accepted and ignored.
  * KCLPP_ORDER=fast in the environment builds the DAG from the bin-sort core
- * order (same degeneracy and clique counts, other ties) instead of SortByCore.
+ * order (same degeneracy and clique counts, other ties) instead of SortByCore;
+ * KCLPP_TUNE=file keeps the autotuned launch schedule in that file (tuned and
+ * written on the first run, loaded on the next ones; no result changes).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -48,8 +50,22 @@ int main(int argc, char **argv) {
   printf("Building the graph structure\n");
   kclpp_graph *g;
   const char *order = getenv("KCLPP_ORDER");  /* "fast": the bin-sort peel */
-  CHECK(kclpp_build_graph_mode(ctx, el, order && !strcmp(order, "fast") ? KCLPP_ORDER_FAST : KCLPP_ORDER_EXACT,
-                               &g));
+  const int order_mode = order && !strcmp(order, "fast") ? KCLPP_ORDER_FAST : KCLPP_ORDER_EXACT;
+  CHECK(kclpp_build_graph_mode(ctx, el, order_mode, &g));
+  const char *tune = getenv("KCLPP_TUNE");  /* schedule cache: loaded when it matches, else tuned and written */
+  if (tune && *tune) {
+    uint64_t h;
+    CHECK(kclpp_edge_list_hash(el, &h));
+    h ^= (uint64_t)order_mode * 0x9E3779B97F4A7C15ull;
+    kclpp_schedule sp;
+    if (kclpp_schedule_load(tune, h, k, KCLPP_KERNEL_ORDER, &sp) == KCLPP_OK) {
+      CHECK(kclpp_graph_set_schedule(ctx, g, &sp));
+    } else {
+      kclpp_tune_result tr;
+      CHECK(kclpp_autotune(ctx, g, k, KCLPP_KERNEL_ORDER, &tr));
+      CHECK(kclpp_schedule_save(tune, h, k, KCLPP_KERNEL_ORDER, &tr.best));
+    }
+  }
   CHECK(kclpp_graph_info(g, &n, &m, &core));
   printf("Core value (max truncated degree) = %u\n", core);
   printf("Number of nodes (degree > 0) = %u\n", n);

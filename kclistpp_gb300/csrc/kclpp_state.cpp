@@ -1,7 +1,7 @@
 // kclpp_state.cpp -- checkpoints of a run: the r (Seq) or rho (Sim) vector with
 // the passes done, k and a hash of the DAG, so that a run resumes where it
 // stopped (the reference only has a commented-out dump of r,
-// kCDensestNoAtom.c:398-401).  Host only.
+// kCDensestNoAtom.c:398-401); binary edge lists; tuned schedules.  Host only.
 //
 // File layout (little-endian): "KCLPPST1", u32 kind, u32 k, u32 passes, u32 n,
 // u64 graph hash, n x 8 bytes of the vector, u64 checksum (FNV-1a of every
@@ -146,6 +146,86 @@ kclpp_status kclpp_read_edge_list_bin(const char *path, kclpp_edge_list **out) {
   el->pairs.resize((size_t)e * 2);
   for (size_t i = 0; i < el->pairs.size(); ++i) el->pairs[i] = get32(&buf[20 + 4 * i]);
   *out = el;
+  return KCLPP_OK;
+}
+
+// Schedule cache: "KCLPPSC1", u64 graph hash, u32 k, u32 kernel, the 19
+// 32-bit fields of kclpp_schedule in declaration order, u64 checksum (FNV-1a
+// of every byte before it).
+namespace {
+constexpr size_t kSchedFields = 19;
+constexpr size_t kSchedBytes = 8 + 8 + 4 + 4 + kSchedFields * 4 + 8;
+
+void schedule_fields(const kclpp_schedule &sp, uint32_t *v) {
+  size_t i = 0;
+  v[i++] = sp.tier_s_max;
+  v[i++] = sp.tier_s_max_seq;
+  v[i++] = sp.m_split1;
+  v[i++] = sp.m_split2;
+  v[i++] = (uint32_t)sp.steal_seq;
+  v[i++] = (uint32_t)sp.steal_count;
+  v[i++] = sp.seq_waves;
+  for (int j = 0; j < 4; ++j) v[i++] = sp.seq_warps[j];
+  v[i++] = (uint32_t)sp.concurrent_tiers;
+  for (int j = 0; j < 4; ++j) v[i++] = sp.count_warps[j];
+  v[i++] = sp.seq_split1;
+  v[i++] = sp.seq_split2;
+  v[i++] = (uint32_t)sp.concurrent_count;
+}
+
+void schedule_from(const uint32_t *v, kclpp_schedule &sp) {
+  size_t i = 0;
+  sp.tier_s_max = v[i++];
+  sp.tier_s_max_seq = v[i++];
+  sp.m_split1 = v[i++];
+  sp.m_split2 = v[i++];
+  sp.steal_seq = (int)v[i++];
+  sp.steal_count = (int)v[i++];
+  sp.seq_waves = v[i++];
+  for (int j = 0; j < 4; ++j) sp.seq_warps[j] = v[i++];
+  sp.concurrent_tiers = (int)v[i++];
+  for (int j = 0; j < 4; ++j) sp.count_warps[j] = v[i++];
+  sp.seq_split1 = v[i++];
+  sp.seq_split2 = v[i++];
+  sp.concurrent_count = (int)v[i++];
+}
+}  // namespace
+
+kclpp_status kclpp_schedule_save(const char *path, uint64_t graph_hash, int k, int kernel, const kclpp_schedule *sp) {
+  if (!path || !sp) return set_error(KCLPP_ERR_INVALID, "kclpp_schedule_save: null argument");
+  unsigned char buf[kSchedBytes];
+  memcpy(buf, "KCLPPSC1", 8);
+  put64(&buf[8], graph_hash);
+  put32(&buf[16], (uint32_t)k);
+  put32(&buf[20], (uint32_t)kernel);
+  uint32_t v[kSchedFields];
+  schedule_fields(*sp, v);
+  for (size_t i = 0; i < kSchedFields; ++i) put32(&buf[24 + 4 * i], v[i]);
+  put64(&buf[kSchedBytes - 8], fnv1a(buf, kSchedBytes - 8));
+  FILE *f = fopen(path, "wb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s for writing", path);
+  const size_t w = fwrite(buf, 1, kSchedBytes, f);
+  const int rc = fclose(f);
+  if (w != kSchedBytes || rc != 0) return set_error(KCLPP_ERR_IO, "write failed: %s", path);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_schedule_load(const char *path, uint64_t graph_hash, int k, int kernel, kclpp_schedule *sp) {
+  if (!path || !sp) return set_error(KCLPP_ERR_INVALID, "kclpp_schedule_load: null argument");
+  FILE *f = fopen(path, "rb");
+  if (!f) return set_error(KCLPP_ERR_IO, "cannot open %s", path);
+  unsigned char buf[kSchedBytes + 1];
+  const size_t got = fread(buf, 1, sizeof buf, f);
+  fclose(f);
+  if (got != kSchedBytes || memcmp(buf, "KCLPPSC1", 8) != 0)
+    return set_error(KCLPP_ERR_IO, "%s is not a kclpp schedule", path);
+  if (get64(&buf[kSchedBytes - 8]) != fnv1a(buf, kSchedBytes - 8))
+    return set_error(KCLPP_ERR_IO, "%s: checksum mismatch", path);
+  if (get64(&buf[8]) != graph_hash || (int)get32(&buf[16]) != k || (int)get32(&buf[20]) != kernel)
+    return set_error(KCLPP_ERR_INVALID, "%s was tuned for another graph, k or kernel", path);
+  uint32_t v[kSchedFields];
+  for (size_t i = 0; i < kSchedFields; ++i) v[i] = get32(&buf[24 + 4 * i]);
+  schedule_from(v, *sp);
   return KCLPP_OK;
 }
 

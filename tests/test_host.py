@@ -381,3 +381,29 @@ def test_c_client_compiles_links_and_runs(tmp_path):
     rank = [int(x) for x in r.stdout.split()]
     el = K.EdgeList.from_pairs([[0, 1], [0, 2], [0, 3], [1, 2], [1, 3], [2, 3], [3, 4]])
     assert rank == K.core_order(el).tolist()
+
+
+def test_schedule_cache_round_trip(tmp_path):
+    """A stored schedule comes back field for field under its key; another
+    graph, k or kernel, a damaged or truncated file are refused."""
+    el = K.chung_lu(2000, 10.0, 2.3, seed=4)
+    h = el.hash()
+    sp = K.Schedule(tier_s_max=32, tier_s_max_seq=16, m_split1=320, m_split2=640, steal_seq=1, steal_count=1,
+                    seq_waves=8, seq_warps=[8, 12, 16, 24], concurrent_tiers=0, count_warps=[8, 16, 24, 32],
+                    seq_split1=384, seq_split2=768, concurrent_count=1)
+    path = tmp_path / "tuned.sched"
+    K.save_schedule(str(path), h, 4, K.KERNEL_SEQ, sp)
+    assert K.load_schedule(str(path), h, 4, K.KERNEL_SEQ).as_dict() == sp.as_dict()
+    for key in [(h ^ 1, 4, K.KERNEL_SEQ), (h, 5, K.KERNEL_SEQ), (h, 4, K.KERNEL_ORDER)]:
+        with pytest.raises(K.KclppError) as e:
+            K.load_schedule(str(path), *key)
+        assert e.value.status == K.ERR_INVALID
+    raw = path.read_bytes()
+    for bad in (raw[:-1], raw[:30] + bytes([raw[30] ^ 0x40]) + raw[31:], b"not a schedule"):
+        path.write_bytes(bad)
+        with pytest.raises(K.KclppError) as e:
+            K.load_schedule(str(path), h, 4, K.KERNEL_SEQ)
+        assert e.value.status == K.ERR_IO
+    with pytest.raises(K.KclppError) as e:
+        K.load_schedule(str(tmp_path / "missing"), h, 4, K.KERNEL_SEQ)
+    assert e.value.status == K.ERR_IO
