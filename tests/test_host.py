@@ -5,6 +5,7 @@ import hashlib
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -407,3 +408,32 @@ def test_schedule_cache_round_trip(tmp_path):
     with pytest.raises(K.KclppError) as e:
         K.load_schedule(str(tmp_path / "missing"), h, 4, K.KERNEL_SEQ)
     assert e.value.status == K.ERR_IO
+
+
+NULL_PROBE = r"""
+import ctypes as C, sys
+sys.path.insert(0, sys.argv[1])
+import kclistpp_gb300 as K
+skip = {"kclpp_status_string", "kclpp_last_error", "kclpp_version", "kclpp_launch_count", "kclpp_create",
+        "kclpp_count_cliques_noalloc"}
+ok = {K.OK, K.ERR_INVALID, K.ERR_NODEVICE, None}
+for name in K.EXPORTED:
+    if name in skip:
+        continue
+    f = getattr(K._lib, name)
+    args = [0 if t in (C.c_int, C.c_uint32, C.c_uint64, C.c_float, C.c_double) else None for t in f.argtypes]
+    r = f(*args)
+    if r not in ok:
+        print("unexpected", name, r)
+        sys.exit(3)
+print("ok")
+"""
+
+
+def test_null_arguments_never_crash():
+    """Every entry point called with null handles and pointers (zero sizes)
+    returns a status -- KCLPP_ERR_INVALID, or OK where there is nothing to do --
+    instead of faulting.  Run in a child process so that a crash fails the
+    test instead of the session."""
+    r = subprocess.run([sys.executable, "-c", NULL_PROBE, ROOT], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (r.returncode, r.stdout[-500:], r.stderr[-500:])
