@@ -539,8 +539,53 @@ static uint64_t seq_pass_impl_masked(const orc_graph *g, int k, uint64_t *rho, i
   return total;
 }
 
+/* Per-root-vertex streams: every root edge of one root vertex s, in (s, t)
+ * order, in one chain from the pass-start r (its increments stay visible to
+ * the later root edges of s); the roots' chains are independent and summed.
+ * Every vertex a chain touches lies in {s} ∪ N+(s). */
+static uint64_t seq_pass_vertex_streams(const orc_graph *g, int k, uint64_t *rho, int threads) {
+  const uint32_t n = g->n;
+  uint64_t total = 0;
+  if (g->e == 0) return 0;
+  uint64_t *delta = (uint64_t *)xcalloc((size_t)n + 1, sizeof(uint64_t));
+  #pragma omp parallel num_threads(threads > 0 ? threads : 1) reduction(+:total)
+  {
+    orc_ws *w = ws_new(g, k);
+    uint64_t *cur = (uint64_t *)xmalloc(((size_t)n + 1) * sizeof(uint64_t));
+    memcpy(cur, rho, (size_t)n * sizeof(uint64_t));
+    uint64_t *acc = (uint64_t *)xcalloc((size_t)n + 1, sizeof(uint64_t));
+    #pragma omp for schedule(dynamic, 1) nowait
+    for (int64_t sv = 0; sv < (int64_t)n; ++sv) {
+      const uint32_t s = (uint32_t)sv;
+      if (g->cd[s] == g->cd[s + 1]) continue;
+      for (uint64_t i = g->cd[s]; i < g->cd[s + 1]; ++i) {
+        const uint32_t t = g->adj[i];
+        const uint32_t ngw = cur[t] < cur[s] ? t : s;
+        make_subgraph(w, g, s, t);
+        total += seq_rec(w, cur, k - 2, ngw);
+      }
+      acc[s] += cur[s] - rho[s];
+      cur[s] = rho[s];
+      for (uint64_t i = g->cd[s]; i < g->cd[s + 1]; ++i) {
+        const uint32_t x = g->adj[i];
+        acc[x] += cur[x] - rho[x];
+        cur[x] = rho[x];
+      }
+    }
+    #pragma omp critical
+    for (uint32_t x = 0; x < n; ++x) delta[x] += acc[x];
+    free(acc);
+    free(cur);
+    ws_free(w);
+  }
+  for (uint32_t x = 0; x < n; ++x) rho[x] += delta[x];
+  free(delta);
+  return total;
+}
+
 static uint64_t seq_pass_impl(const orc_graph *g, int k, uint64_t *rho, int mode, int threads,
                               uint64_t stride) {
+  if (mode == ORC_SEQ_VERTEX_STREAMS) return seq_pass_vertex_streams(g, k, rho, threads);
   return seq_pass_impl_masked(g, k, rho, mode, threads, stride, NULL);
 }
 

@@ -48,7 +48,8 @@ typedef struct {
 enum {
   ORC_SEQ_SEQUENTIAL = 0,  /* one chain over all root edges: the reference at p = 1 */
   ORC_SEQ_EDGE_STREAMS = 1,/* each root edge its own chain from the pass-start r   */
-  ORC_SEQ_THREADS = 2      /* the reference's own p-thread dynamic schedule (timing only) */
+  ORC_SEQ_THREADS = 2,     /* the reference's own p-thread dynamic schedule (timing only) */
+  ORC_SEQ_VERTEX_STREAMS = 3 /* each root vertex's root edges in one chain from the pass-start r */
 };
 
 /* ---- A1-A4: graph input, degeneracy order, DAG ------------------------- */

@@ -17,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libkclpp_oracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 
-SEQ_SEQUENTIAL, SEQ_EDGE_STREAMS, SEQ_THREADS = 0, 1, 2
+SEQ_SEQUENTIAL, SEQ_EDGE_STREAMS, SEQ_THREADS, SEQ_VERTEX_STREAMS = 0, 1, 2, 3
 
 
 def build(ref: bool = False) -> None:
