@@ -5,7 +5,7 @@ reference) and the orderings of oracle/ordering_study.c.
 
 TEST INFRASTRUCTURE ONLY: an analysis script, not part of the library.
 
-    python oracle/ordering_study.py            # both tables (about 15 minutes on 8 cores)
+    python oracle/ordering_study.py            # both tables (about 5 minutes on 8 cores)
     python oracle/ordering_study.py --table b  # the live-load simulation only
 
 Table A (k = 5, RMAT scale 13 with 4 planted G(n_c, 0.5) communities): the
