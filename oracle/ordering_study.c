@@ -195,3 +195,67 @@ uint64_t orc_list_cliques(const orc_graph *g, int k, uint32_t *buf, uint64_t cap
   ws_free(w);
   return L.cnt;
 }
+
+/* One pass of P streams sharing one load vector, simulated: stream j walks
+ * its root edges (stream_edges[stream_first[j] .. stream_first[j + 1]), each
+ * edge's cliques cl[ef[e] .. ef[e + 1]) in order).  The streams advance in
+ * steps of `chunk` cliques; inside a step a stream sees the loads as the
+ * previous step left them plus its own increments of this step, and gives
+ * each clique's unit to its member of smallest load (ties to the earlier
+ * member of the row); the step's increments are added at its end.  The
+ * result does not depend on the order in which the streams of a step run. */
+void orc_sim_shared_pass(int k, const uint32_t *cl, const uint64_t *ef, const uint32_t *stream_edges,
+                         const uint64_t *stream_first, uint32_t P, uint32_t chunk, uint64_t *loads, int threads) {
+  uint64_t *pos_edge = (uint64_t *)xmalloc((size_t)P * sizeof(uint64_t));  /* index into stream_edges */
+  uint64_t *pos_cl = (uint64_t *)xmalloc((size_t)P * sizeof(uint64_t));    /* next clique of that edge */
+  uint32_t *inc = (uint32_t *)xmalloc((size_t)P * chunk * sizeof(uint32_t));
+  uint32_t *ninc = (uint32_t *)xcalloc(P, sizeof(uint32_t));
+  for (uint32_t j = 0; j < P; ++j) {
+    pos_edge[j] = stream_first[j];
+    pos_cl[j] = pos_edge[j] < stream_first[j + 1] ? ef[stream_edges[pos_edge[j]]] : 0;
+  }
+  int active = 1;
+  while (active) {
+    active = 0;
+    #pragma omp parallel for num_threads(threads > 0 ? threads : 1) schedule(dynamic, 64) reduction(|:active)
+    for (int64_t jj = 0; jj < (int64_t)P; ++jj) {
+      const uint32_t j = (uint32_t)jj;
+      uint32_t *my = inc + (size_t)j * chunk;
+      uint32_t cnt = 0;
+      while (cnt < chunk && pos_edge[j] < stream_first[j + 1]) {
+        const uint32_t e = stream_edges[pos_edge[j]];
+        if (pos_cl[j] >= ef[e + 1]) {  /* next root edge of this stream */
+          pos_edge[j]++;
+          if (pos_edge[j] < stream_first[j + 1]) pos_cl[j] = ef[stream_edges[pos_edge[j]]];
+          continue;
+        }
+        const uint32_t *row = cl + pos_cl[j] * (uint64_t)k;
+        uint32_t best = row[0];
+        uint64_t bv = loads[best];
+        for (uint32_t q = 0; q < cnt; ++q) bv += my[q] == best;
+        for (int a = 1; a < k; ++a) {
+          const uint32_t x = row[a];
+          uint64_t xv = loads[x];
+          for (uint32_t q = 0; q < cnt; ++q) xv += my[q] == x;
+          if (xv < bv) {
+            best = x;
+            bv = xv;
+          }
+        }
+        my[cnt++] = best;
+        pos_cl[j]++;
+      }
+      ninc[j] = cnt;
+      if (cnt) active = 1;
+    }
+    for (uint32_t j = 0; j < P; ++j) {
+      const uint32_t *my = inc + (size_t)j * chunk;
+      for (uint32_t q = 0; q < ninc[j]; ++q) loads[my[q]]++;
+      ninc[j] = 0;
+    }
+  }
+  free(pos_edge);
+  free(pos_cl);
+  free(inc);
+  free(ninc);
+}

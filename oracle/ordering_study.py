@@ -5,8 +5,8 @@ reference) and the orderings of oracle/ordering_study.c.
 
 TEST INFRASTRUCTURE ONLY: an analysis script, not part of the library.
 
-    python oracle/ordering_study.py            # both tables (about 5 minutes on 8 cores)
-    python oracle/ordering_study.py --table b  # the live-load simulation only
+    python oracle/ordering_study.py            # all three tables (about 6 minutes on 8 cores)
+    python oracle/ordering_study.py --table b  # the shared-load simulation on a small graph only
 
 Table A (k = 5, RMAT scale 13 with 4 planted G(n_c, 0.5) communities): the
 reference's sequential order, the library's per-root-edge streams and waves,
@@ -23,6 +23,9 @@ loads once per 32 cliques of a stream (the stream sees only its own
 increments inside a chunk).  The same number of cliques per pass; every
 clique still gives one unit to one member, so r / T stays a feasible load
 and the bound a certificate.
+
+Table C: the shared-load simulation of table B, in C, on the graph of table
+A (1e8 cliques per pass), up to a GB300's 7,296 resident warps as streams.
 """
 from __future__ import annotations
 
@@ -60,6 +63,7 @@ def study_lib() -> C.CDLL:
         "orc_seq_pass_hybrid": (None, [G, C.c_int, u64p, C.c_uint32, C.c_int]),
         "orc_seq_find_densest": (O.OrcInfo, [G, C.c_int, C.c_uint32, u64p, u32p, u32p, C.c_int]),
         "orc_list_cliques": (C.c_uint64, [G, C.c_int, u32p, C.c_uint64, u64p]),
+        "orc_sim_shared_pass": (None, [C.c_int, u32p, u64p, u32p, u64p, C.c_uint32, C.c_uint32, u64p, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -97,6 +101,46 @@ class Study:
 
     def ptr(self, r):
         return r.ctypes.data_as(C.POINTER(C.c_uint64))
+
+
+def list_cliques(L, S):
+    cnt = L.orc_list_cliques(S.g, S.k, None, 0, None)
+    cl = np.zeros((cnt, S.k), np.uint32)
+    ef = np.zeros(S.e + 1, np.uint64)
+    L.orc_list_cliques(S.g, S.k, cl.ctypes.data_as(C.POINTER(C.c_uint32)), cnt,
+                       ef.ctypes.data_as(C.POINTER(C.c_uint64)))
+    return cl, ef
+
+
+def stream_schedule(ef, e, P):
+    """Root edges in order, each to the stream that frees first (a GPU's
+    dynamic schedule), as CSR: stream_first[P + 1], stream_edges."""
+    sizes = np.diff(ef).astype(np.int64)
+    heap = [(0, j) for j in range(P)]
+    lists = [[] for _ in range(P)]
+    for i in range(e):
+        if sizes[i] == 0:
+            continue
+        t, j = heapq.heappop(heap)
+        lists[j].append(i)
+        heapq.heappush(heap, (t + int(sizes[i]), j))
+    first = np.zeros(P + 1, np.uint64)
+    first[1:] = np.cumsum([len(x) for x in lists])
+    edges = np.array([i for x in lists for i in x], dtype=np.uint32)
+    return edges, first
+
+
+def shared_step(L, S, cl, ef, P, chunk):
+    edges, first = stream_schedule(ef, S.e, P)
+    edges = edges if len(edges) else np.zeros(1, np.uint32)
+
+    def step(r, T):
+        L.orc_sim_shared_pass(S.k, cl.ctypes.data_as(C.POINTER(C.c_uint32)),
+                              ef.ctypes.data_as(C.POINTER(C.c_uint64)),
+                              edges.ctypes.data_as(C.POINTER(C.c_uint32)),
+                              first.ctypes.data_as(C.POINTER(C.c_uint64)), P, chunk, S.ptr(r), 8)
+
+    return step
 
 
 def table_a(L) -> None:
@@ -200,21 +244,39 @@ def table_b(L) -> None:
         rows.append((f"{P} streams in lock step, shared loads", lockstep(P, 1)))
     for P in (256, 1024, 4096):
         rows.append((f"{P} streams, shared loads read every 32 cliques", lockstep(P, 32)))
+    rows.append(("256 streams, every 32 cliques (the C simulation of table C)",
+                 shared_step(L, S, cl, ef, 256, 32)))
     for name, step in rows:
         t0 = time.time()
         print(f"  {name:62s} {S.passes(step, 300):>24s}   ({time.time() - t0:.0f} s)", flush=True)
 
 
+def table_c(L) -> None:
+    """Shared loads at a larger scale: the graph of table A (1.0e8 5-cliques per
+    pass), with up to a GB300's resident warps (152 SMs x 48) as streams."""
+    el = K.rmat_planted(13, 16, 4, 60, 150, 0.5, seed=79)
+    S = Study(L, el, 5)
+    cl, ef = list_cliques(L, S)
+    print(f"Table C: k = 5, {S.n} vertices, {S.e} root edges, {len(cl)} cliques per pass")
+    for P in (1024, 7296, 32768):
+        t0 = time.time()
+        res = S.passes(shared_step(L, S, cl, ef, P, 32), 200)
+        print(f"  {P:6d} streams, shared loads read every 32 cliques {res:>34s}   ({time.time() - t0:.0f} s)",
+              flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--table", choices=["a", "b", "both"], default="both")
+    ap.add_argument("--table", choices=["a", "b", "c", "all"], default="all")
     a = ap.parse_args()
     L = study_lib()
     print(f"passes to a certified {100 * GAP:.0f} % gap (ub / density - 1)")
-    if a.table in ("a", "both"):
+    if a.table in ("a", "all"):
         table_a(L)
-    if a.table in ("b", "both"):
+    if a.table in ("b", "all"):
         table_b(L)
+    if a.table in ("c", "all"):
+        table_c(L)
 
 
 if __name__ == "__main__":
