@@ -112,13 +112,16 @@ def list_cliques(L, S):
     return cl, ef
 
 
-def stream_schedule(ef, e, P):
-    """Root edges in order, each to the stream that frees first (a GPU's
+def stream_schedule(ef, e, P, by_work=False):
+    """Root edges in (s, t) order -- or by decreasing clique count, the order
+    the kernels take roots in -- each to the stream that frees first (a GPU's
     dynamic schedule), as CSR: stream_first[P + 1], stream_edges."""
     sizes = np.diff(ef).astype(np.int64)
     heap = [(0, j) for j in range(P)]
     lists = [[] for _ in range(P)]
-    for i in range(e):
+    order = np.argsort(-sizes, kind="stable") if by_work else range(e)
+    for i in order:
+        i = int(i)
         if sizes[i] == 0:
             continue
         t, j = heapq.heappop(heap)
@@ -130,8 +133,8 @@ def stream_schedule(ef, e, P):
     return edges, first
 
 
-def shared_step(L, S, cl, ef, P, chunk):
-    edges, first = stream_schedule(ef, S.e, P)
+def shared_step(L, S, cl, ef, P, chunk, by_work=False):
+    edges, first = stream_schedule(ef, S.e, P, by_work)
     edges = edges if len(edges) else np.zeros(1, np.uint32)
 
     def step(r, T):
@@ -258,11 +261,12 @@ def table_c(L) -> None:
     S = Study(L, el, 5)
     cl, ef = list_cliques(L, S)
     print(f"Table C: k = 5, {S.n} vertices, {S.e} root edges, {len(cl)} cliques per pass")
-    for P in (1024, 7296, 32768):
+    for P, by_work in ((1024, False), (7296, False), (32768, False), (7296, True)):
         t0 = time.time()
-        res = S.passes(shared_step(L, S, cl, ef, P, 32), 200)
-        print(f"  {P:6d} streams, shared loads read every 32 cliques {res:>34s}   ({time.time() - t0:.0f} s)",
-              flush=True)
+        res = S.passes(shared_step(L, S, cl, ef, P, 32, by_work), 200)
+        order = "by decreasing work" if by_work else "in (s, t) order"
+        print(f"  {P:6d} streams, shared loads every 32 cliques, root edges {order:18s} {res:>8s}"
+              f"   ({time.time() - t0:.0f} s)", flush=True)
 
 
 def main() -> None:
