@@ -13,6 +13,7 @@
  * KCLPP_TUNE=file keeps the autotuned launch schedule in that file (tuned and
  * written on the first run, loaded on the next ones; no result changes).
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime under a strict C standard */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>

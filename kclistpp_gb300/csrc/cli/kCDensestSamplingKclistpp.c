@@ -17,6 +17,7 @@
  *   KCLPP_ORDER=fast      the bin-sort core order instead of SortByCore's
  * Times are wall-clock milliseconds.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime under a strict C standard */
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
