@@ -331,7 +331,10 @@ kclpp_status kclpp_edge_list_hash(const kclpp_edge_list *el, uint64_t *hash);
  * sum equals the unsharded pass exactly (integers). */
 /* owner[v] = rank that processes root v (greedy by out-degree squared). */
 kclpp_status kclpp_shard_plan(uint32_t n, const uint64_t *offsets, uint32_t world, uint32_t *owner);
-/* Restrict g's root schedule to `rank`'s share (world = 1 restores all roots). */
+/* Restrict g's root schedule to `rank`'s share (world = 1 restores all roots).
+ * While g is sharded (world > 1) only kclpp_seq_delta_dev and
+ * kclpp_sim_counts_dev accept it; every other entry point that runs over the
+ * graph's roots returns KCLPP_ERR_INVALID rather than a partial result. */
 kclpp_status kclpp_graph_shard(kclpp_ctx *ctx, kclpp_graph *g, uint32_t rank, uint32_t world);
 /* Seq pass increments of g's roots from r (device): delta = r_after - r, for
  * this shard only (CDF_CliqueEnum FRANK_WOLFE, kCDensestNoAtom.c:270-295). */

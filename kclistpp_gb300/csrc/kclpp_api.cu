@@ -507,6 +507,17 @@ static kclpp_status check_k(int k, int lo) {
   return KCLPP_OK;
 }
 
+// After kclpp_graph_shard(world > 1) the graph's root schedule holds this
+// rank's roots only, so a whole-graph result would silently be partial: only
+// the shard entry points (kclpp_seq_delta_dev, kclpp_sim_counts_dev) accept a
+// sharded graph; kclpp_graph_shard(ctx, g, 0, 1) restores the full schedule.
+static kclpp_status check_unsharded(const kclpp_graph *g, const char *fn) {
+  if (g->shard_world > 1)
+    return set_error(KCLPP_ERR_INVALID, "%s: the graph is sharded (rank %u of %u); only kclpp_seq_delta_dev and "
+                     "kclpp_sim_counts_dev run on a shard", fn, g->shard_rank, g->shard_world);
+  return KCLPP_OK;
+}
+
 // ---- host-side pieces of the extraction (A10, A12, A13) --------------------
 struct KeyId {
   uint64_t key;
@@ -725,6 +736,7 @@ void kclpp_graph_free(kclpp_graph *g) {
 // ---- counts ---------------------------------------------------------------------
 kclpp_status kclpp_count_cliques(kclpp_ctx *c, const kclpp_graph *gc, int k, uint64_t *per_vertex, uint64_t *total) {
   if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_count_cliques"));
   KCL_TRY(check_k(k, 3));
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
@@ -760,6 +772,7 @@ static kclpp_status seq_passes_on(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t 
 kclpp_status kclpp_seq_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t passes, int det_mode,
                                   uint64_t *r_dev) {
   if (!c || !gc || (!r_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_seq_passes_dev"));
   KCL_TRY(check_k(k, 3));
   if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
     return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
@@ -770,6 +783,7 @@ kclpp_status kclpp_seq_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, ui
 kclpp_status kclpp_seq_passes(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t passes, int det_mode,
                               uint64_t *r) {
   if (!c || !gc || (!r && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_seq_passes"));
   KCL_TRY(check_k(k, 3));
   if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
     return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
@@ -795,6 +809,7 @@ kclpp_status kclpp_seq_passes_csr(kclpp_ctx *c, uint32_t n, uint64_t m, const ui
 // ---- Sim --------------------------------------------------------------------------
 kclpp_status kclpp_sim_counts(kclpp_ctx *c, const kclpp_graph *gc, int k, const double *rho, uint64_t *cnt) {
   if (!c || !gc || ((!rho || !cnt) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_sim_counts"));
   KCL_TRY(check_k(k, 2));
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
@@ -809,6 +824,7 @@ kclpp_status kclpp_sim_counts(kclpp_ctx *c, const kclpp_graph *gc, int k, const 
 kclpp_status kclpp_sim_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t t_first, uint32_t passes,
                                   double *rho_dev) {
   if (!c || !gc || (!rho_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_sim_passes_dev"));
   KCL_TRY(check_k(k, 2));
   if (t_first < 1) return set_error(KCLPP_ERR_INVALID, "t_first must be >= 1");
   KCL_TRY(set_device(c));
@@ -820,6 +836,7 @@ kclpp_status kclpp_sim_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, ui
 kclpp_status kclpp_sim_passes(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t t_first, uint32_t passes,
                               double *rho) {
   if (!c || !gc || (!rho && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_sim_passes"));
   KCL_TRY(check_k(k, 2));
   if (t_first < 1) return set_error(KCLPP_ERR_INVALID, "t_first must be >= 1");
   KCL_TRY(set_device(c));
@@ -998,6 +1015,7 @@ static kclpp_status time_tiers(kclpp_ctx *c, kclpp_graph *g, int k, int mode, st
 
 kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kclpp_tune_result *out) {
   if (!c || !g || !out) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(g, "kclpp_autotune"));
   if (kernel != KCLPP_KERNEL_SEQ && kernel != KCLPP_KERNEL_ORDER)
     return set_error(KCLPP_ERR_INVALID, "autotune: kernel must be KCLPP_KERNEL_SEQ or KCLPP_KERNEL_ORDER");
   KCL_TRY(check_k(k, kernel == KCLPP_KERNEL_SEQ ? 3 : 2));
@@ -1317,6 +1335,7 @@ kclpp_status kclpp_sort_by_r_f64(kclpp_ctx *c, uint32_t n, const double *r, uint
 
 kclpp_status kclpp_pava(kclpp_ctx *c, const kclpp_graph *gc, int k, const uint32_t *level, uint64_t *tentative) {
   if (!c || !gc || ((!level || !tentative) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_pava"));
   KCL_TRY(check_k(k, 2));
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
@@ -1385,9 +1404,49 @@ static kclpp_status edges_in_prefix(kclpp_ctx *c, kclpp_graph *g, uint32_t nstar
   return KCLPP_OK;
 }
 
+extern "C++" {
+// The upper bound of kCDensestNoAtom.c:352-369 (Seq) and kCDensestCmpSync.c:
+// 365-381 (Sim): walk the vertices in load order, the running binomial
+// C(i+1, k) against the prefix's load; next_load(i) adds the i-th vertex and
+// returns the prefix load as the reference computes it (Seq: the integer sum
+// divided by T; Sim: the FP64 sum), so the FP operations are the reference's.
+template <typename NextLoad>
+static double upper_bound_scan(uint32_t n, int k, NextLoad next_load) {
+  double ub = 0, ip1ck = 1;
+  for (uint32_t i = 0; i < n; ++i) {
+    const double load = next_load(i);
+    if (i + 1 == (uint32_t)k) ip1ck = 1;
+    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
+    if (ip1ck < load) ub = ip1ck / (i + 1);
+    else {
+      if (ub < load / (i + 1)) ub = load / (i + 1);
+      break;
+    }
+  }
+  return ub;
+}
+
+// kCDensestNoAtom.c:342-349: the first strictly largest prefix density of the
+// exact prefix clique counts (integer accumulator).
+static void densest_prefix_u64(const std::vector<uint64_t> &tent, kclpp_densest_info *info) {
+  double density = -1;
+  unsigned long long sum = 0;
+  for (uint32_t i = 0; i < (uint32_t)tent.size(); ++i) {
+    sum += tent[i];
+    if ((double)sum / (i + 1) > density) {
+      density = (double)sum / (i + 1);
+      info->n = i + 1;
+      info->cliques = sum;
+    }
+  }
+  info->density = density;
+}
+}  // extern "C++"
+
 kclpp_status kclpp_extract_densest_seq(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t T, const uint64_t *r,
                                        kclpp_densest_info *info, uint32_t *reordered_out) {
   if (!c || !gc || !info || (!r && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_extract_densest_seq"));
   KCL_TRY(check_k(k, 3));
   if (T < 1) return set_error(KCLPP_ERR_INVALID, "T must be >= 1");
   KCL_TRY(set_device(c));
@@ -1399,33 +1458,13 @@ kclpp_status kclpp_extract_densest_seq(kclpp_ctx *c, const kclpp_graph *gc, int 
   KCL_TRY(kclpp_sort_by_r_u64(c, n, r, reordered.data(), level.data()));
   std::vector<uint64_t> tent;
   KCL_TRY(pava_and_edges(c, g, k, level, tent));
-  // kCDensestNoAtom.c:342-349: first strictly largest prefix density.
-  double density = -1;
-  unsigned long long sum = 0;
-  for (uint32_t i = 0; i < n; ++i) {
-    sum += tent[i];
-    if ((double)sum / (i + 1) > density) {
-      density = (double)sum / (i + 1);
-      info->n = i + 1;
-      info->cliques = sum;
-    }
-  }
-  info->density = density;
+  densest_prefix_u64(tent, info);
   KCL_TRY(edges_in_prefix(c, g, info->n, &info->m));
-  // kCDensestNoAtom.c:352-369
-  sum = 0;
-  double ub = 0, ip1ck = 1;
-  for (uint32_t i = 0; i < n; ++i) {
+  unsigned long long sum = 0;
+  info->ub = upper_bound_scan(n, k, [&](uint32_t i) {
     sum += r[reordered[i]];
-    if (i + 1 == (uint32_t)k) ip1ck = 1;
-    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
-    if (ip1ck < (double)sum / T) ub = ip1ck / (i + 1);
-    else {
-      if (ub < (double)sum / T / (i + 1)) ub = (double)sum / T / (i + 1);
-      break;
-    }
-  }
-  info->ub = ub;
+    return (double)sum / T;
+  });
   if (reordered_out) memcpy(reordered_out, reordered.data(), (size_t)n * 4);
   return KCLPP_OK;
 }
@@ -1433,6 +1472,7 @@ kclpp_status kclpp_extract_densest_seq(kclpp_ctx *c, const kclpp_graph *gc, int 
 kclpp_status kclpp_extract_densest_sim(kclpp_ctx *c, const kclpp_graph *gc, int k, const double *rho,
                                        kclpp_densest_info *info, uint32_t *reordered_out) {
   if (!c || !gc || !info || (!rho && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_extract_densest_sim"));
   KCL_TRY(check_k(k, 2));
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
@@ -1457,20 +1497,11 @@ kclpp_status kclpp_extract_densest_sim(kclpp_ctx *c, const kclpp_graph *gc, int 
   }
   info->density = density;
   KCL_TRY(edges_in_prefix(c, g, info->n, &info->m));
-  // kCDensestCmpSync.c:365-381
   sum = 0;
-  double ub = 0, ip1ck = 1;
-  for (uint32_t i = 0; i < n; ++i) {
+  info->ub = upper_bound_scan(n, k, [&](uint32_t i) {
     sum += rho[reordered[i]];
-    if (i + 1 == (uint32_t)k) ip1ck = 1;
-    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
-    if (ip1ck < sum) ub = ip1ck / (i + 1);
-    else {
-      if (ub < sum / (i + 1)) ub = sum / (i + 1);
-      break;
-    }
-  }
-  info->ub = ub;
+    return sum;
+  });
   if (reordered_out) memcpy(reordered_out, reordered.data(), (size_t)n * 4);
   return KCLPP_OK;
 }
@@ -1479,6 +1510,7 @@ kclpp_status kclpp_extract_densest_sim(kclpp_ctx *c, const kclpp_graph *gc, int 
 kclpp_status kclpp_seq_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t num_iter, int det_mode,
                             uint64_t *r_out, kclpp_densest_info *infos, int max_infos, int *n_infos) {
   if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_seq_main"));
   KCL_TRY(check_k(k, 3));
   if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
     return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
@@ -1512,6 +1544,7 @@ kclpp_status kclpp_seq_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t
 kclpp_status kclpp_sim_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t num_iter, double *rho_out,
                             kclpp_densest_info *infos, int max_infos, int *n_infos) {
   if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_sim_main"));
   KCL_TRY(check_k(k, 2));
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
@@ -1596,6 +1629,7 @@ extern "C" {
 
 kclpp_status kclpp_warm_features(kclpp_ctx *c, const kclpp_graph *gc, float *X_dev) {
   if (!c || !gc || (!X_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_warm_features"));
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
   const uint32_t n = g->dag.n;
@@ -1643,6 +1677,7 @@ kclpp_status kclpp_warm_start_r(kclpp_ctx *c, const kclpp_graph *gc, const kclpp
 kclpp_status kclpp_extract_densest_seq_warm(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t T,
                                             const uint64_t *r, const uint64_t *r0, kclpp_densest_info *info) {
   if (!c || !gc || !info || ((!r || !r0) && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
+  KCL_TRY(check_unsharded(gc, "kclpp_extract_densest_seq_warm"));
   KCL_TRY(check_k(k, 3));
   if (T < 1) return set_error(KCLPP_ERR_INVALID, "T must be >= 1");
   KCL_TRY(set_device(c));
@@ -1656,17 +1691,7 @@ kclpp_status kclpp_extract_densest_seq_warm(kclpp_ctx *c, const kclpp_graph *gc,
   KCL_TRY(kclpp_sort_by_r_u64(c, n, r, reordered.data(), level.data()));
   std::vector<uint64_t> tent;
   KCL_TRY(pava_and_edges(c, g, k, level, tent));
-  double density = -1;
-  unsigned long long sum = 0;
-  for (uint32_t i = 0; i < n; ++i) {
-    sum += tent[i];
-    if ((double)sum / (i + 1) > density) {
-      density = (double)sum / (i + 1);
-      info->n = i + 1;
-      info->cliques = sum;
-    }
-  }
-  info->density = density;
+  densest_prefix_u64(tent, info);
   KCL_TRY(edges_in_prefix(c, g, info->n, &info->m));
   // Upper bound from the loads the T passes added: (r - r0) / T is a feasible
   // fractional assignment of the cliques (every pass gives each clique one
@@ -1675,19 +1700,11 @@ kclpp_status kclpp_extract_densest_seq_warm(kclpp_ctx *c, const kclpp_graph *gc,
   std::vector<uint64_t> inc(n);
   for (uint32_t i = 0; i < n; ++i) inc[i] = r[i] - r0[i];
   std::sort(inc.begin(), inc.end(), std::greater<uint64_t>());
-  sum = 0;
-  double ub = 0, ip1ck = 1;
-  for (uint32_t i = 0; i < n; ++i) {
+  unsigned long long sum = 0;
+  info->ub = upper_bound_scan(n, k, [&](uint32_t i) {
     sum += inc[i];
-    if (i + 1 == (uint32_t)k) ip1ck = 1;
-    else if (i + 1 > (uint32_t)k) ip1ck = (ip1ck * (i + 1)) / (i + 1 - k);
-    if (ip1ck < (double)sum / T) ub = ip1ck / (i + 1);
-    else {
-      if (ub < (double)sum / T / (i + 1)) ub = (double)sum / T / (i + 1);
-      break;
-    }
-  }
-  info->ub = ub;
+    return (double)sum / T;
+  });
   return KCLPP_OK;
 }
 

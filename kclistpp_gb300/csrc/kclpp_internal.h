@@ -3,6 +3,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/kclpp.h"
@@ -36,6 +37,64 @@ struct SplitMix {
 
 // Stable LSD radix sort of 64-bit keys (16-bit digits, only the digits that vary).
 void radix_sort_u64(std::vector<uint64_t> &keys);
+
+// Indexed binary min-heap with the operation order of the reference's heaps
+// (BinaryHeap.c:6-90 and the u64 heap of kClistCoreTrim.c:445-526): the same
+// swaps in the same sequence, so ties pop in the reference's order.  The tie
+// order defines the degeneracy order (hence the DAG and every Seq r) and the
+// k-clique core peel's order, which is why it has to be the same algorithm.
+struct PeelHeap {
+  std::vector<uint32_t> pos;  // key -> position (UINT32_MAX once popped)
+  std::vector<uint32_t> key;  // position -> key
+  std::vector<uint64_t> val;  // position -> value
+  uint32_t n = 0;
+  explicit PeelHeap(uint32_t nmax) : pos(nmax, UINT32_MAX), key(nmax), val(nmax) {}
+  inline void swap_at(uint32_t i, uint32_t j) {
+    std::swap(pos[key[i]], pos[key[j]]);
+    std::swap(key[i], key[j]);
+    std::swap(val[i], val[j]);
+  }
+  inline void up(uint32_t i) {
+    while (i > 0) {
+      const uint32_t j = (i - 1) >> 1;
+      if (val[j] > val[i]) { swap_at(i, j); i = j; }
+      else break;
+    }
+  }
+  inline void down() {
+    uint32_t i = 0;
+    for (;;) {
+      const uint32_t j1 = 2 * i + 1, j2 = j1 + 1;
+      if (j1 >= n) break;
+      const uint32_t j = (j2 < n && val[j2] < val[j1]) ? j2 : j1;
+      if (val[j] < val[i]) { swap_at(i, j); i = j; }
+      else break;
+    }
+  }
+  inline void push(uint32_t k, uint64_t v) {
+    pos[k] = n;
+    key[n] = k;
+    val[n] = v;
+    ++n;
+    up(n - 1);
+  }
+  inline void dec(uint32_t k, uint64_t d) {
+    const uint32_t i = pos[k];
+    if (i != UINT32_MAX) { val[i] -= d; up(i); }
+  }
+  inline uint32_t pop(uint64_t *v) {
+    const uint32_t k = key[0];
+    if (v) *v = val[0];
+    pos[k] = UINT32_MAX;
+    --n;
+    key[0] = key[n];
+    val[0] = val[n];
+    pos[key[0]] = 0;  // as the reference: re-points the last key even when n hits 0
+    down();
+    return k;
+  }
+  inline bool live(uint32_t k) const { return pos[k] != UINT32_MAX; }
+};
 
 // Host DAG in CSR form.
 struct HostDag {

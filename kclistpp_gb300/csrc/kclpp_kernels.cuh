@@ -982,35 +982,52 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
 
 }  // namespace dev
 
-// Per-kernel launch settings, computed once per (kernel, dynamic shared
-// memory size): the opt-in shared-memory attribute and the number of CTAs one
-// SM holds.  Launches then cost no runtime queries.
+// Per-kernel launch settings, computed once per (device, kernel, dynamic
+// shared memory size): the opt-in shared-memory attribute (a per-device
+// setting: cudaFuncSetAttribute applies to the current device only) and the
+// number of CTAs one SM holds.  Launches then cost no runtime queries.
+constexpr int kMaxDevices = 64;
 struct LaunchCache {
   std::mutex mu;
-  int attr_bytes = -1;
+  int attr_bytes[kMaxDevices];
   size_t occ_smem[64];  // fixed storage: launching never touches the heap
+  int occ_dev[64];
   int occ_threads[64];
   int occ_ctas[64];
   int nocc = 0;
-  // Seq tiers M / L: chosen warps per CTA by (out-degree bound, requested width).
+  // Seq tiers M / L: chosen warps per CTA by (device, out-degree bound, requested width).
   uint32_t nw_dmax[32];
-  int nw_req[32], nw_val[32];
+  int nw_dev[32], nw_req[32], nw_val[32];
   int nnw = 0;
+  LaunchCache() {
+    for (int i = 0; i < kMaxDevices; ++i) attr_bytes[i] = -1;
+  }
 };
+
+static inline int current_device() {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) d = 0;
+  return d;
+}
 
 template <typename Fn>
 static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int *per_sm) {
+  const int dev = current_device();
   std::lock_guard<std::mutex> g(lc.mu);
-  if ((int)smem > lc.attr_bytes) {
+  if ((int)smem > lc.attr_bytes[dev]) {
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    lc.attr_bytes = (int)smem;
+    lc.attr_bytes[dev] = (int)smem;
   }
   for (int i = 0; i < lc.nocc; ++i)
-    if (lc.occ_smem[i] == smem && lc.occ_threads[i] == threads) { *per_sm = lc.occ_ctas[i]; return cudaSuccess; }
+    if (lc.occ_dev[i] == dev && lc.occ_smem[i] == smem && lc.occ_threads[i] == threads) {
+      *per_sm = lc.occ_ctas[i];
+      return cudaSuccess;
+    }
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, smem) != cudaSuccess || nb < 1) nb = 1;
   if (lc.nocc < 64) {
+    lc.occ_dev[lc.nocc] = dev;
     lc.occ_smem[lc.nocc] = smem;
     lc.occ_threads[lc.nocc] = threads;
     lc.occ_ctas[lc.nocc] = nb;
@@ -1028,10 +1045,14 @@ template <int MODE, int K, typename Fn>
 static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
   using namespace dev;
   constexpr int lo = 8, hi = warps_m<MODE, K>(), step = MODE == MODE_SEQ ? 4 : 8;
+  const int dev = current_device();
   {
     std::lock_guard<std::mutex> g(lc.mu);
     for (int i = 0; i < lc.nnw; ++i)
-      if (lc.nw_dmax[i] == dmax && lc.nw_req[i] == req) { *nw = lc.nw_val[i]; return cudaSuccess; }
+      if (lc.nw_dev[i] == dev && lc.nw_dmax[i] == dmax && lc.nw_req[i] == req) {
+        *nw = lc.nw_val[i];
+        return cudaSuccess;
+      }
   }
   int best = 0, best_warps = -1;
   for (int w = lo; w <= hi; w += step) {
@@ -1046,6 +1067,7 @@ static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_i
   if (best == 0) best = req > hi ? hi : lo;  // a width this launch cannot take: the nearest one
   std::lock_guard<std::mutex> g(lc.mu);
   if (lc.nnw < 32) {
+    lc.nw_dev[lc.nnw] = dev;
     lc.nw_dmax[lc.nnw] = dmax;
     lc.nw_req[lc.nnw] = req;
     lc.nw_val[lc.nnw] = best;

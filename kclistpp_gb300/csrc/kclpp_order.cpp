@@ -3,70 +3,15 @@
 // SortByCore (Graph.c:57-91) is a sequential min-degree peel whose tie order
 // comes from the binary heap of BinaryHeap.c:6-90; the DAG orientation, and
 // with it every clique's enumeration order and every Seq-kClist++ r value,
-// depends on that order.  The heap below performs the same swaps in the same
-// sequence (an implementation of the same algorithm, not a copy), so the rank
-// permutation is identical to the reference's.
+// depends on that order.  PeelHeap (kclpp_internal.h) performs the same swaps
+// in the same sequence (an implementation of the same algorithm, not a copy),
+// so the rank permutation is identical to the reference's.
 #include <algorithm>
 #include <cstring>
 
 #include "kclpp_internal.h"
 
 namespace kclpp {
-
-namespace {
-struct Heap {
-  // key -> position (UINT32_MAX once popped), position -> (key, value)
-  std::vector<uint32_t> pos;
-  std::vector<uint32_t> key;
-  std::vector<uint64_t> val;
-  uint32_t n = 0;
-  explicit Heap(uint32_t nmax) : pos(nmax, UINT32_MAX), key(nmax), val(nmax) {}
-  inline void swap_at(uint32_t i, uint32_t j) {
-    std::swap(pos[key[i]], pos[key[j]]);
-    std::swap(key[i], key[j]);
-    std::swap(val[i], val[j]);
-  }
-  inline void up(uint32_t i) {
-    while (i > 0) {
-      uint32_t j = (i - 1) >> 1;
-      if (val[j] > val[i]) { swap_at(i, j); i = j; }
-      else break;
-    }
-  }
-  inline void down() {
-    uint32_t i = 0;
-    for (;;) {
-      uint32_t j1 = 2 * i + 1, j2 = j1 + 1;
-      if (j1 >= n) break;
-      uint32_t j = (j2 < n && val[j2] < val[j1]) ? j2 : j1;
-      if (val[j] < val[i]) { swap_at(i, j); i = j; }
-      else break;
-    }
-  }
-  inline void push(uint32_t k, uint64_t v) {
-    pos[k] = n;
-    key[n] = k;
-    val[n] = v;
-    ++n;
-    up(n - 1);
-  }
-  inline void dec(uint32_t k, uint64_t d) {
-    uint32_t i = pos[k];
-    if (i != UINT32_MAX) { val[i] -= d; up(i); }
-  }
-  inline uint32_t pop(uint64_t *v) {
-    uint32_t k = key[0];
-    if (v) *v = val[0];
-    pos[k] = UINT32_MAX;
-    --n;
-    key[0] = key[n];
-    val[0] = val[n];
-    pos[key[0]] = 0;  // as the reference: re-points the last key even when n hits 0
-    down();
-    return k;
-  }
-};
-}  // namespace
 
 // Undirected CSR of an edge list (both directions of every pair).
 static void undirected_csr(uint32_t n, const std::vector<uint32_t> &pairs, std::vector<uint64_t> &cd,
@@ -88,7 +33,7 @@ void core_peel_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *or
   std::vector<uint64_t> cd;
   std::vector<uint32_t> adj;
   undirected_csr(n, pairs, cd, adj);
-  Heap h(n);
+  PeelHeap h(n);
   for (uint32_t i = 0; i < n; ++i) h.push(i, cd[i + 1] - cd[i]);
   for (uint32_t i = 0; i < n; ++i) {
     uint64_t v = 0;

@@ -8,6 +8,7 @@
 // byte before it).
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "kclpp_internal.h"
@@ -141,11 +142,19 @@ kclpp_status kclpp_read_edge_list_bin(const char *path, kclpp_edge_list **out) {
     return set_error(KCLPP_ERR_IO, "%s: truncated edge list", path);
   if (get64(&buf[buf.size() - 8]) != fnv1a(buf.data(), buf.size() - 8))
     return set_error(KCLPP_ERR_IO, "%s: checksum mismatch", path);
-  auto *el = new kclpp_edge_list();
-  el->n = get32(&buf[8]);
+  const uint32_t n = get32(&buf[8]);
+  std::unique_ptr<kclpp_edge_list> el(new kclpp_edge_list());
+  el->n = n;
   el->pairs.resize((size_t)e * 2);
-  for (size_t i = 0; i < el->pairs.size(); ++i) el->pairs[i] = get32(&buf[20 + 4 * i]);
-  *out = el;
+  // The checksum only catches accidental damage: a file written with a wrong
+  // n passes it, and every later stage indexes arrays of n entries by these
+  // ids, so each id is checked against n.
+  for (size_t i = 0; i < el->pairs.size(); ++i) {
+    const uint32_t v = get32(&buf[20 + 4 * i]);
+    if (v >= n) return set_error(KCLPP_ERR_IO, "%s: vertex id %u is not below the stored n = %u", path, v, n);
+    el->pairs[i] = v;
+  }
+  *out = el.release();
   return KCLPP_OK;
 }
 

@@ -36,49 +36,6 @@ struct kclpp_trim_result {
 
 namespace {
 
-struct Peel {
-  // indexed min-heap with the reference's operation order (see kclpp_order.cpp)
-  std::vector<uint32_t> pos, key;
-  std::vector<uint64_t> val;
-  uint32_t n = 0;
-  explicit Peel(uint32_t nmax) : pos(nmax, UINT32_MAX), key(nmax), val(nmax) {}
-  void swap_at(uint32_t i, uint32_t j) {
-    std::swap(pos[key[i]], pos[key[j]]);
-    std::swap(key[i], key[j]);
-    std::swap(val[i], val[j]);
-  }
-  void up(uint32_t i) {
-    while (i > 0) {
-      uint32_t j = (i - 1) >> 1;
-      if (val[j] > val[i]) { swap_at(i, j); i = j; }
-      else break;
-    }
-  }
-  void down() {
-    uint32_t i = 0;
-    for (;;) {
-      uint32_t j1 = 2 * i + 1, j2 = j1 + 1;
-      if (j1 >= n) break;
-      uint32_t j = (j2 < n && val[j2] < val[j1]) ? j2 : j1;
-      if (val[j] < val[i]) { swap_at(i, j); i = j; }
-      else break;
-    }
-  }
-  void push(uint32_t k, uint64_t v) { pos[k] = n; key[n] = k; val[n] = v; ++n; up(n - 1); }
-  void dec(uint32_t k, uint64_t d) { uint32_t i = pos[k]; if (i != UINT32_MAX) { val[i] -= d; up(i); } }
-  uint32_t pop(uint64_t *v) {
-    uint32_t k = key[0];
-    *v = val[0];
-    pos[k] = UINT32_MAX;
-    --n;
-    key[0] = key[n]; val[0] = val[n];
-    pos[key[0]] = 0;
-    down();
-    return k;
-  }
-  bool live(uint32_t k) const { return pos[k] != UINT32_MAX; }
-};
-
 inline uint32_t isect(const uint32_t *a, uint32_t na, const uint32_t *b, uint32_t nb, uint32_t *out) {
   uint32_t i = 0, j = 0, s = 0;
   while (i < na && j < nb) {
@@ -208,7 +165,7 @@ kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int
   std::vector<uint32_t> rank(n), map(n);
   uint32_t n2 = n;
   {
-    Peel h(n);
+    PeelHeap h(n);
     for (uint32_t i = 0; i < n; ++i) h.push(i, cd0[i + 1] - cd0[i]);
     uint32_t r = 0, c = 0;
     const uint32_t kk = (uint32_t)kmax - 1;
@@ -283,7 +240,7 @@ kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int
   std::vector<char> alive(n2, 0);
   if (mode == KCLPP_TRIM_EXACT) {
     // kcliquecore (:605-666)
-    Peel h(n2);
+    PeelHeap h(n2);
     for (uint32_t i = 0; i < n2; ++i) h.push(i, R->nck[i]);
     uint64_t c = 0, ncktot = tot;
     uint32_t ecount = (uint32_t)e2;  // `unsigned e` in the reference

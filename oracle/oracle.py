@@ -20,9 +20,28 @@ REF_DIR = os.path.join(HERE, "_ref")
 SEQ_SEQUENTIAL, SEQ_EDGE_STREAMS, SEQ_THREADS, SEQ_VERTEX_STREAMS = 0, 1, 2, 3
 
 
-def build(ref: bool = False) -> None:
-    """make the oracle library (and, with ref=True, the reference programs)."""
-    targets = ["all"] + (["ref"] if ref else [])
+# Where the reference's C sources are read from when the reference programs
+# are compiled (the golden-vector generators and build()); KCLPP_REFERENCE_SRC
+# overrides it.  Only that compile step reads there; nothing at test or bench
+# time does.
+_REFERENCE_SRC_DEFAULT = "/root/reference"
+
+
+def reference_sources() -> str | None:
+    """The directory holding the reference's sources, or None where it is absent."""
+    d = os.environ.get("KCLPP_REFERENCE_SRC", _REFERENCE_SRC_DEFAULT)
+    return d if os.path.isdir(d) else None
+
+
+def build(ref: bool = False, ref_if_present: bool = False) -> None:
+    """make the oracle library; with ref=True also the reference programs
+    (which must then be present), with ref_if_present=True wherever they are."""
+    targets = ["all"]
+    src = reference_sources()
+    if ref and not src:
+        raise RuntimeError("the reference sources are not present (set KCLPP_REFERENCE_SRC)")
+    if (ref or ref_if_present) and src:
+        targets += ["ref", "REF=" + src]
     r = subprocess.run(["make", "-s", "-C", HERE] + targets, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)

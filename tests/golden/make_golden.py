@@ -32,6 +32,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 REF = os.path.join(ROOT, "oracle", "_ref")
 sys.path.insert(0, ROOT)
 
+from oracle import oracle as O  # noqa: E402
 from tests.golden.cases import CASES, make_pairs  # noqa: E402
 
 
@@ -90,7 +91,7 @@ def trim_ref(path: str, k: int) -> dict:
 
 
 def main() -> None:
-    run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"])
+    O.build(ref=True)
     index = {}
     for case in CASES:
         name = case["name"]

@@ -99,7 +99,7 @@ def check_line(rep: dict, line: list) -> None:
 
 
 def main() -> None:
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
+    O.build(ref=True)
     index, arrays = {}, {}
     for case in CASES:
         name = case["name"]

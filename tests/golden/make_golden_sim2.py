@@ -22,12 +22,13 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 REF = os.path.join(ROOT, "oracle", "_ref")
 sys.path.insert(0, ROOT)
 
+from oracle import oracle as O  # noqa: E402
 from tests.golden.cases import CASES, make_pairs  # noqa: E402
 from tests.golden.make_golden import parse_cmpsync  # noqa: E402
 
 
 def main() -> None:
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "all", "ref"], check=True)
+    O.build(ref=True)
     index, arrays = {}, {}
     T = 16
     for case in CASES:

@@ -25,6 +25,7 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 REF = os.path.join(ROOT, "oracle", "_ref")
 sys.path.insert(0, ROOT)
 
+from oracle import oracle as O  # noqa: E402
 from tests.golden.cases import CASES, make_pairs  # noqa: E402
 
 
@@ -36,7 +37,7 @@ def extra_cases():
 
 
 def main() -> None:
-    subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"], check=True)
+    O.build(ref=True)
     graphs = [(c["name"], make_pairs(c)) for c in CASES] + extra_cases()
     index, arrays = {}, {}
     for name, pairs in graphs:

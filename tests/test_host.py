@@ -296,6 +296,33 @@ def test_binary_edge_list_cache(tmp_path):
         assert e.value.status == K.ERR_IO
 
 
+def _fnv1a(data: bytes) -> int:
+    h = 0xCBF29CE484222325
+    for b in data:
+        h = ((h ^ b) * 0x100000001B3) & 0xFFFFFFFFFFFFFFFF
+    return h
+
+
+def test_binary_edge_list_ids_checked_against_n(tmp_path):
+    """A binary edge list whose stored n is too small for its ids is refused,
+    even when its checksum is consistent (the checksum only detects damage)."""
+    import struct
+
+    pairs = np.array([[0, 1], [1, 5], [2, 3]], dtype=np.uint32)
+    for n, ok in ((6, True), (5, False), (1, False)):
+        body = b"KCLPPEL1" + struct.pack("<IQ", n, len(pairs)) + pairs.astype("<u4").tobytes()
+        q = str(tmp_path / f"n{n}.bin")
+        open(q, "wb").write(body + struct.pack("<Q", _fnv1a(body)))
+        if ok:
+            back = K.EdgeList.read_bin(q)
+            assert back.n == n and np.array_equal(back.pairs(), pairs)
+        else:
+            with pytest.raises(K.KclppError) as e:
+                K.EdgeList.read_bin(q)
+            assert e.value.status == K.ERR_IO
+            assert b"not below" in K._lib.kclpp_last_error()
+
+
 def test_trim_k2_matches_reference():
     """k = 2 (NormalGraphCoreTrim.c): vertices kept, edges kept and the trimmed
     edge list, in input order, equal to the reference program's output files

@@ -110,6 +110,10 @@ def test_split_pass_on_gpu(ctx):
             ctx.synchronize()
             acc_c += part
             torch.cuda.synchronize()
+        # a whole-graph entry point refuses a sharded graph (its result would be partial)
+        with pytest.raises(K.KclppError) as e:
+            K.seq_passes(g, k, 1, r0)
+        assert e.value.status == K.ERR_INVALID and b"sharded" in K._lib.kclpp_last_error()
         K.graph_shard(g, 0, 1)
         assert np.array_equal(r0 + acc_r.cpu().numpy().view(np.uint64), full_r)
         assert np.array_equal(acc_c.cpu().numpy().view(np.uint64), full_c)
