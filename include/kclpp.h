@@ -430,6 +430,9 @@ kclpp_status kclpp_extract_densest_seq_warm(kclpp_ctx *ctx, const kclpp_graph *g
                                best suffix and trimmed set identical to it */
 #define KCLPP_TRIM_FAST 1   /* GPU density-threshold trimming: the rho-core for the
                                best density seen; no core numbers */
+#define KCLPP_TRIM_EXACT_HOST 2 /* the same peel as EXACT with every recount on the
+                               host, one pop at a time (the reference's own loop;
+                               kept as the check of EXACT) */
 typedef struct kclpp_trim_result kclpp_trim_result;
 typedef struct {
   uint32_t n, n2;        /* input vertices; vertices with core >= k-1          */
@@ -457,6 +460,17 @@ kclpp_status kclpp_trim_info_get(const kclpp_trim_result *t, kclpp_trim_info *in
  * (the ckcore file, :672-676).  Any output may be NULL. */
 kclpp_status kclpp_trim_copy(const kclpp_trim_result *t, uint32_t *map, uint64_t *nck,
                              uint32_t *order, uint64_t *core_num);
+/* How the EXACT peel's recounts ran (no reference counterpart): the heap's pops
+ * are the reference's, one at a time on the host; the recounts of a batch of
+ * predicted pops run together on the GPU and a pop commits only when it is the
+ * predicted one.  batches: GPU rounds; predicted / committed: pops predicted and
+ * committed; gpu_roots / host_roots: committed pops recounted on the GPU / on the
+ * host (more than 2048 live neighbours); seconds: wall time of the peel. */
+typedef struct {
+  uint64_t batches, predicted, committed, gpu_roots, host_roots;
+  double seconds;
+} kclpp_peel_stats;
+kclpp_status kclpp_trim_peel_stats(const kclpp_trim_result *t, kclpp_peel_stats *st);
 /* The trimmed graph in original ids and input order (printdensest, :686-699). */
 kclpp_status kclpp_trim_edges(const kclpp_trim_result *t, kclpp_edge_list **out);
 void kclpp_trim_free(kclpp_trim_result *t);

@@ -39,7 +39,7 @@ ERR_INVALID, ERR_IO, ERR_NOMEM, ERR_CUDA, ERR_UNSUPPORTED, ERR_OVERFLOW, ERR_NOD
 MAX_K = 8
 SEQ_EDGE_STREAMS = 1
 SEQ_WAVES = 2
-TRIM_EXACT, TRIM_FAST = 0, 1
+TRIM_EXACT, TRIM_FAST, TRIM_EXACT_HOST = 0, 1, 2
 ORDER_EXACT, ORDER_FAST = 0, 1
 SAMPLE_TARGET = 10_000_000  # the reference's CLIQUES_TO_SAMPLE
 GEN_CHUNG_LU, GEN_RMAT, GEN_ER, GEN_PLANTED, GEN_RMAT_PLANTED = 1, 2, 3, 4, 5
@@ -68,6 +68,14 @@ class TrimInfo(C.Structure):
                 ("core", C.c_uint32), ("total", C.c_uint64), ("ckcore", C.c_uint64),
                 ("ckrho", C.c_double), ("rho", C.c_double), ("size", C.c_uint32),
                 ("ntrim", C.c_uint32), ("mtrim", C.c_uint64), ("ncktrim", C.c_uint64)]
+
+
+class PeelStats(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("predicted", C.c_uint64), ("committed", C.c_uint64),
+                ("gpu_roots", C.c_uint64), ("host_roots", C.c_uint64), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
 
 
 class StateInfo(C.Structure):
@@ -232,6 +240,7 @@ _SIGS = {
     "kclpp_trim_info_get": (C.c_int, [_P, C.POINTER(TrimInfo)]),
     "kclpp_trim_copy": (C.c_int, [_P, _u32p, _u64p, _u32p, _u64p]),
     "kclpp_trim_edges": (C.c_int, [_P, C.POINTER(_P)]),
+    "kclpp_trim_peel_stats": (C.c_int, [_P, C.POINTER(PeelStats)]),
     "kclpp_trim_free": (None, [_P]),
     "kclpp_sampling_create": (C.c_int, [_P, _P, C.c_int, C.c_uint64, C.c_uint64, C.c_uint32, C.POINTER(_P)]),
     "kclpp_sampling_info_get": (C.c_int, [_P, C.POINTER(SamplingInfo)]),
@@ -715,6 +724,7 @@ class TrimResult:
     order: np.ndarray      # peel order (new labels)
     core_num: np.ndarray   # core number along the peel order
     edges: EdgeList        # trimmed graph, original ids, input order
+    peel: PeelStats | None = None  # how the EXACT peel's recounts ran
 
 
 def trim(ctx: Context | None, el: EdgeList, k: int, mode: int = TRIM_EXACT) -> TrimResult:
@@ -733,7 +743,9 @@ def trim(ctx: Context | None, el: EdgeList, k: int, mode: int = TRIM_EXACT) -> T
                                     _ptr(core, C.c_uint64)))
         eh = _P()
         _check(_lib.kclpp_trim_edges(h, C.byref(eh)))
-        return TrimResult(info, mp, nck, order, core, EdgeList(eh))
+        ps = PeelStats()
+        _check(_lib.kclpp_trim_peel_stats(h, C.byref(ps)))
+        return TrimResult(info, mp, nck, order, core, EdgeList(eh), ps)
     finally:
         _lib.kclpp_trim_free(h)
 

@@ -33,7 +33,7 @@ CXXFLAGS = ["-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-un
 NVCCFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
 
-CU_SOURCES = ["kclpp_api.cu", "kclpp_k_count.cu", "kclpp_k_order.cu", "kclpp_k_seq.cu", "kclpp_warm.cu", "kclpp_sample.cu"]
+CU_SOURCES = ["kclpp_api.cu", "kclpp_k_count.cu", "kclpp_k_order.cu", "kclpp_k_seq.cu", "kclpp_warm.cu", "kclpp_sample.cu", "kclpp_peel.cu"]
 CPP_SOURCES = ["kclpp_gen.cpp", "kclpp_order.cpp", "kclpp_trim.cpp", "kclpp_state.cpp", "kclpp_exact.cpp"]
 PROGRAMS = ["kCDensestNoAtom", "kCDensestCmpSync", "kClistCoreTrim", "NormalGraphCoreTrim", "kCDensestSamplingKclistpp"]
 

@@ -1575,6 +1575,8 @@ cudaStream_t ctx_stream(kclpp_ctx *c) { return c->stream; }
 int ctx_device(kclpp_ctx *c) { return c->device; }
 int ctx_sms(kclpp_ctx *c) { return c->num_sms; }
 void ctx_count_launch(kclpp_ctx *c, int n) { c->launches += (uint64_t)n; }
+uint32_t *ctx_err_word(kclpp_ctx *c) { return c->d_err; }
+kclpp_status ctx_check_err(kclpp_ctx *c) { return check_err(c); }
 const HostDag &graph_dag(const kclpp_graph *g) { return g->dag; }
 const uint64_t *graph_dev_offsets(const kclpp_graph *g) { return g->d_off; }
 const uint32_t *graph_dev_cols(const kclpp_graph *g) { return g->d_cols; }

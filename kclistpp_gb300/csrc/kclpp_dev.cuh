@@ -53,7 +53,30 @@ struct PassArgs {
   uint64_t slab_words;            // words per CTA in slab
   uint32_t deg_lo, deg_hi;        // id-order schedules: out-degree window of this launch
   unsigned long long *total;      // id-order schedules: sum of the roots' own clique counts
+  // MODE_COUNT over explicit member lists (the k-clique core peel's recounts):
+  // when list_off is set, root s is an index into list_off / list_cols, its
+  // members are list_cols[list_off[s] .. list_off[s + 1]) (ascending ids, the
+  // induced rows still built from the DAG off / cols), and the number of
+  // k-cliques of {root} ∪ members through member i is stored at
+  // pair_out[list_off[s] + i] instead of being added to out[].
+  const uint64_t *list_off;
+  const uint32_t *list_cols;
+  unsigned long long *pair_out;
 };
+
+// A root's member list: its DAG out-list, or its explicit list (peel recounts).
+__device__ __forceinline__ void root_span(const PassArgs &a, uint32_t s, uint64_t &o, int &d,
+                                          const uint32_t *&cols) {
+  if (a.list_off) {
+    o = a.list_off[s];
+    d = (int)(a.list_off[s + 1] - o);
+    cols = a.list_cols;
+  } else {
+    o = a.off[s];
+    d = (int)(a.off[s + 1] - o);
+    cols = a.cols;
+  }
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;

@@ -110,11 +110,23 @@ cudaStream_t ctx_stream(kclpp_ctx *c);
 int ctx_device(kclpp_ctx *c);
 int ctx_sms(kclpp_ctx *c);
 void ctx_count_launch(kclpp_ctx *c, int n);
+uint32_t *ctx_err_word(kclpp_ctx *c);
+// Reads (and clears) the device status word after synchronising the stream.
+kclpp_status ctx_check_err(kclpp_ctx *c);
 // Graph accessors for the same: the host DAG and its device copy.
 const HostDag &graph_dag(const kclpp_graph *g);
 const uint64_t *graph_dev_offsets(const kclpp_graph *g);
 const uint32_t *graph_dev_cols(const kclpp_graph *g);
 int graph_device(const kclpp_graph *g);
+
+// Recounts of the k-clique core peel on the GPU (kclpp_peel.cu): for a batch
+// of roots with explicit member lists (live neighbours, ascending), the
+// k-cliques through each root and member, for the roots flagged in gpu[].
+struct PeelRecount;
+kclpp_status peel_recount_create(kclpp_ctx *c, const kclpp_graph *g, int k, PeelRecount **out);
+kclpp_status peel_recount_run(PeelRecount *P, uint32_t nroots, const uint64_t *loff, const uint32_t *lcols,
+                              const uint8_t *gpu, uint64_t *w);
+void peel_recount_free(PeelRecount *P);
 
 // SortByCore with the reference heap's tie order.
 void core_order_host(uint32_t n, const std::vector<uint32_t> &pairs, uint32_t *rank);

@@ -156,8 +156,10 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
     idx = __shfl_sync(KCL_FULL, idx, 0);
     if (idx >= a.num_roots) break;
     const uint32_t s = IDENT ? idx : a.roots[idx];
-    const uint64_t o = a.off[s];
-    const int d = (int)(a.off[s + 1] - o);
+    uint64_t o;
+    int d;
+    const uint32_t *lcols;
+    root_span(a, s, o, d, lcols);
     if constexpr (IDENT) {
       if ((uint32_t)d < a.deg_lo || (uint32_t)d > a.deg_hi) continue;
     }
@@ -166,7 +168,7 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
       continue;
     }
     if (d < K - 1 || d == 0) continue;
-    for (int i = lane; i < d; i += 32) sm.list[i] = a.cols[o + i];
+    for (int i = lane; i < d; i += 32) sm.list[i] = lcols[o + i];
     int tau = 0;
     if constexpr (MODE == MODE_ORDER) {
       for (int i = lane; i < d; i += 32) sm.base[i] = vertex_key(a, sm.list[i]);
@@ -270,11 +272,12 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
       uint64_t tot = 0;
       for (int x = lane; x < d; x += 32) {
         const uint64_t c = cnt64<K - 2, true>(sm.rows[x], sm.rows);
-        if (c) atomicAdd(&a.out[sm.list[x]], (unsigned long long)c);
+        if (a.list_off) a.pair_out[o + x] = (unsigned long long)c;
+        else if (c) atomicAdd(&a.out[sm.list[x]], (unsigned long long)c);
         tot += c;
       }
       tot = warp_sum(tot);
-      if (lane == 0 && tot) {
+      if (lane == 0 && tot && !a.list_off) {
         atomicAdd(&a.out[s], (unsigned long long)(tot / (K - 1)));
         if constexpr (IDENT) atomicAdd(a.total, (unsigned long long)(tot / (K - 1)));
       }
@@ -773,7 +776,7 @@ __device__ __forceinline__ uint32_t find_victim(const PassArgs &a, int need, int
     const uint32_t idx = *(volatile uint32_t *)(a.active + b);
     if (idx >= a.num_roots) continue;
     const uint32_t s = IDENT ? idx : a.roots[idx];
-    const uint32_t d = (uint32_t)(a.off[s + 1] - a.off[s]);
+    const uint32_t d = a.list_off ? (uint32_t)(a.list_off[s + 1] - a.list_off[s]) : (uint32_t)(a.off[s + 1] - a.off[s]);
     const uint32_t taken = *(volatile uint32_t *)(a.task_next + idx);
     const bool in_window = !IDENT || (d >= a.deg_lo && d <= a.deg_hi && d <= a.dmax);
     if (in_window && (int)d >= need && taken + kMinSteal <= d && d - taken > best) {
@@ -843,8 +846,16 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
     if (idx == UINT32_MAX) break;
     uint32_t *next = a.task_next + idx;  // root's sub-task counter, shared by every CTA on it
     const uint32_t s = IDENT ? idx : a.roots[idx];
-    const uint64_t o = a.off[s];
-    const int d = (int)(a.off[s + 1] - o);
+    uint64_t o;
+    int d;
+    const uint32_t *lcols;
+    if constexpr (MODE == MODE_COUNT) {
+      root_span(a, s, o, d, lcols);
+    } else {
+      o = a.off[s];
+      d = (int)(a.off[s + 1] - o);
+      lcols = a.cols;
+    }
     if constexpr (IDENT) {
       if ((uint32_t)d < a.deg_lo || (uint32_t)d > a.deg_hi) {
         __syncthreads();
@@ -862,7 +873,7 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
     }
     const int W = (d + 31) >> 5;
     const int row_words = MODE == MODE_SEQ ? (int)tri_off((uint32_t)d) : d * W;
-    for (int i = tid; i < d; i += NW * 32) list[i] = a.cols[o + i];
+    for (int i = tid; i < d; i += NW * 32) list[i] = lcols[o + i];
     for (int i = tid; i < row_words; i += NW * 32) rows[i] = 0;
     if constexpr (MODE == MODE_ORDER) {
       for (int i = tid; i < d; i += NW * 32) base[i] = vertex_key(a, a.cols[o + i]);
@@ -959,7 +970,8 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
         }
         if (lane == 0) {
           if (MODE == MODE_COUNT) {
-            if (c) atomicAdd(&a.out[list[p]], (unsigned long long)c);
+            if (a.list_off) a.pair_out[o + p] = (unsigned long long)c;
+            else if (c) atomicAdd(&a.out[list[p]], (unsigned long long)c);
             mine += c_low;
           } else if (p < tau) {
             if (c) atomicAdd(&a.out[list[inv[p]]], (unsigned long long)c);
@@ -970,7 +982,7 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
       }
       if (lane == 0 && mine) atomicAdd(&s_sum, mine);
       __syncthreads();
-      if (tid == 0 && s_sum) {
+      if (tid == 0 && s_sum && !(MODE == MODE_COUNT && a.list_off)) {
         atomicAdd(&a.out[s], s_sum);
         if constexpr (IDENT && MODE == MODE_COUNT) atomicAdd(a.total, s_sum);
       }

@@ -10,12 +10,18 @@
 //                that DAG (onepass, :394-416)
 //   peel         EXACT: the reference's k-clique-degree heap peel with a local
 //                recount around every popped vertex (kcliquecore/oneshortpass,
-//                :577-666) -- sequential by definition, run on the host;
+//                :577-666): the heap's pops are sequential by definition and
+//                stay on the host, the recounts run on the GPU in speculative
+//                batches of predicted pops (a pop commits only when it is the
+//                predicted one, so the result is the reference's bit for bit);
+//                EXACT_HOST: the same peel with every recount on the host, one
+//                pop at a time (the check of EXACT);
 //                FAST: GPU rounds that drop every vertex whose k-clique degree
 //                is below the best density seen and recount, ending at the
 //                rho-core for that density
 //   output       trimmed edges in original ids and input order (:686-699)
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -32,6 +38,7 @@ struct kclpp_trim_result {
   std::vector<uint32_t> order;
   std::vector<uint64_t> core_num;
   std::vector<uint32_t> trimmed;  // pairs, original ids
+  kclpp_peel_stats peel{};
 };
 
 namespace {
@@ -67,6 +74,129 @@ struct Rec {
       size[k - 2] = isect(adj + cd[x], (uint32_t)(cd[x + 1] - cd[x]), &merge[t], size[k - 3], &merge[t2]);
       run(k + 1);
     }
+  }
+};
+
+// The bookkeeping of kcliquecore (kClistCoreTrim.c:605-666) for one pop: the
+// running core number, the peel order, the edge count, the heap decrements in
+// the order of the popped vertex's adjacency (updateLLU per live neighbour)
+// and the best suffix density.
+struct PeelBook {
+  uint32_t n2;
+  uint64_t kmax;
+  kclpp_trim_info &I;
+  kclpp_trim_result &R;
+  uint64_t c = 0, ncktot;
+  uint32_t ecount;  // `unsigned e` in the reference
+  uint32_t i = 0;   // pops committed
+  std::vector<uint64_t> whendel;
+  PeelBook(uint32_t n2_, int k, kclpp_trim_info &I_, kclpp_trim_result &R_, uint64_t tot, uint64_t e2)
+      : n2(n2_), kmax((uint64_t)k), I(I_), R(R_), ncktot(tot), ecount((uint32_t)e2), whendel((size_t)n2_ + 1, 0) {
+    I.ncktrim = tot;
+    I.ckrho = (double)ncktot / (double)n2;
+    I.size = n2;
+    I.rho = (double)(2 * ecount) / (double)(n2 * (n2 - 1));
+  }
+  // u popped with degree v; A = its live neighbours (ascending), W = the
+  // k-cliques through u and each of them among the live vertices.
+  void commit(PeelHeap &h, uint32_t u, uint64_t v, const uint32_t *A, uint32_t na, const uint64_t *W) {
+    if (v > c) c = v;
+    R.order[i] = u;
+    R.core_num[i] = c;
+    uint64_t ncktot2 = 0;
+    for (uint32_t q = 0; q < na; ++q) {
+      ecount--;
+      h.dec(A[q], W[q]);
+      ncktot2 += W[q];
+    }
+    const uint32_t size_tmp = n2 - i - 1;
+    whendel[size_tmp] = ncktot2 / (kmax - 1);  // every clique is seen by k - 1 neighbours
+    ncktot -= whendel[size_tmp];
+    const double ckrho_tmp = (double)ncktot / (double)size_tmp;
+    if (ckrho_tmp > I.ckrho) {
+      I.ckrho = ckrho_tmp;
+      I.size = size_tmp;
+      I.rho = (double)(2 * ecount) / (double)(size_tmp * (size_tmp - 1));
+    }
+    ++i;
+  }
+  // The last vertex, the trimmed set (the vertices alive before the first
+  // deletion of degree >= ckrho) and its clique count.
+  void finish(PeelHeap &h, std::vector<char> &alive) {
+    I.ntrim = n2;  // the reference leaves ntrim unset when n2 == 1
+    for (uint32_t j = n2 - 1; j >= 1; --j) {
+      if ((double)whendel[j] >= I.ckrho) { I.ntrim = j + 1; break; }
+      I.ncktrim -= whendel[j];
+    }
+    uint64_t v;
+    R.order[i] = h.pop(&v);
+    R.core_num[i] = c;
+    I.ckcore = c;
+    for (uint32_t q = n2 - 1; q != n2 - I.ntrim - 1; --q) alive[R.order[q]] = 1;
+  }
+};
+
+// oneshortpass on the host (kClistCoreTrim.c:577-603): the k-cliques through
+// u and each live neighbour A[q], from the DAG recursion; nck2 is an all-zero
+// scratch vector of n2 entries and is left all zero.
+void recount_host(Rec &rec, uint32_t u, const uint32_t *A, uint32_t na, uint64_t *nck2, uint64_t *W) {
+  for (uint32_t q = 0; q < na; ++q) W[q] = 0;
+  if (na <= rec.kmax - 2) return;
+  rec.nck = nck2;
+  rec.ck[0] = u;
+  for (uint32_t q = 0; q < na; ++q) {
+    const uint32_t w = A[q];
+    rec.ck[1] = w;
+    rec.size[0] = isect(A, na, rec.adj + rec.cd[w], (uint32_t)(rec.cd[w + 1] - rec.cd[w]), rec.merge.data());
+    rec.run(3);
+  }
+  for (uint32_t q = 0; q < na; ++q) {
+    W[q] = nck2[A[q]];
+    nck2[A[q]] = 0;
+  }
+  nck2[u] = 0;
+}
+
+// A read-only view of a PeelHeap that can pop without changing it (the pops
+// land in a stamped overlay): the next pops the heap would make if no degree
+// changed, i.e. the prediction of a speculative batch.
+struct HeapPeek {
+  const PeelHeap &h;
+  std::vector<uint32_t> st, ok;
+  std::vector<uint64_t> ov;
+  uint32_t gen = 0, n = 0;
+  explicit HeapPeek(const PeelHeap &h_) : h(h_), st(h_.key.size(), 0), ok(h_.key.size()), ov(h_.key.size()) {}
+  void reset() {
+    if (++gen == 0) {
+      std::fill(st.begin(), st.end(), 0);
+      gen = 1;
+    }
+    n = h.n;
+  }
+  uint32_t K(uint32_t i) const { return st[i] == gen ? ok[i] : h.key[i]; }
+  uint64_t V(uint32_t i) const { return st[i] == gen ? ov[i] : h.val[i]; }
+  void set(uint32_t i, uint32_t k, uint64_t v) { st[i] = gen; ok[i] = k; ov[i] = v; }
+  // PeelHeap::pop's sequence of moves, positions only.
+  uint32_t pop() {
+    const uint32_t k0 = K(0);
+    --n;
+    set(0, K(n), V(n));
+    uint32_t i = 0;
+    for (;;) {
+      const uint32_t j1 = 2 * i + 1, j2 = j1 + 1;
+      if (j1 >= n) break;
+      const uint32_t j = (j2 < n && V(j2) < V(j1)) ? j2 : j1;
+      if (V(j) < V(i)) {
+        const uint32_t ki = K(i), kj = K(j);
+        const uint64_t vi = V(i), vj = V(j);
+        set(i, kj, vj);
+        set(j, ki, vi);
+        i = j;
+      } else {
+        break;
+      }
+    }
+    return k0;
   }
 };
 
@@ -135,12 +265,12 @@ static kclpp_status trim_k2(const kclpp_edge_list *el, kclpp_trim_result **out) 
 kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int mode, kclpp_trim_result **out) {
   if (!el || !out) return set_error(KCLPP_ERR_INVALID, "kclpp_trim: null argument");
   *out = nullptr;
-  if (mode != KCLPP_TRIM_EXACT && mode != KCLPP_TRIM_FAST) return set_error(KCLPP_ERR_INVALID, "unknown trim mode");
+  if (mode != KCLPP_TRIM_EXACT && mode != KCLPP_TRIM_FAST && mode != KCLPP_TRIM_EXACT_HOST)
+    return set_error(KCLPP_ERR_INVALID, "unknown trim mode");
   if (kmax == 2) return trim_k2(el, out);
   if (!ctx) return set_error(KCLPP_ERR_INVALID, "kclpp_trim: null context (needed for k >= 3)");
   if (kmax < 3 || kmax > KCLPP_MAX_K)
     return set_error(KCLPP_ERR_UNSUPPORTED, "k = %d outside [2, %d]", kmax, KCLPP_MAX_K);
-  if (mode != KCLPP_TRIM_EXACT && mode != KCLPP_TRIM_FAST) return set_error(KCLPP_ERR_INVALID, "unknown trim mode");
   std::unique_ptr<kclpp_trim_result> R(new kclpp_trim_result());
   kclpp_trim_info &I = R->info;
   memset(&I, 0, sizeof I);
@@ -238,18 +368,21 @@ kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int
     for (uint32_t i = 0; i < n2; ++i) std::sort(au.begin() + cu[i], au.begin() + cu[i + 1]);
   }
   std::vector<char> alive(n2, 0);
-  if (mode == KCLPP_TRIM_EXACT) {
-    // kcliquecore (:605-666)
+  if (mode == KCLPP_TRIM_EXACT || mode == KCLPP_TRIM_EXACT_HOST) {
+    // kcliquecore (:605-666): the reference's heap and its pops, one at a
+    // time.  EXACT_HOST recounts each popped vertex on the host as the
+    // reference does.  EXACT predicts the heap's next B pops (what it would
+    // pop if no degree changed), recounts all of them at once on the GPU with
+    // each one's live set as it would be at its pop, then commits pops while
+    // the heap's actual minimum is the predicted vertex: a committed pop's
+    // live set is then exactly the predicted one, so its counts are exact.
+    // The first pop that differs ends the batch; its count is recomputed in
+    // the next one.  B doubles while whole batches commit and shrinks to
+    // what the last batch committed otherwise.
+    const auto t_peel = std::chrono::steady_clock::now();
     PeelHeap h(n2);
     for (uint32_t i = 0; i < n2; ++i) h.push(i, R->nck[i]);
-    uint64_t c = 0, ncktot = tot;
-    uint32_t ecount = (uint32_t)e2;  // `unsigned e` in the reference
-    std::vector<uint64_t> whendel((size_t)n2 + 1, 0), nck2((size_t)n2 + 1, 0);
-    std::vector<uint32_t> live((size_t)n2 + 1);
-    I.ncktrim = tot;
-    I.ckrho = (double)ncktot / (double)n2;
-    I.size = n2;
-    I.rho = (double)(2 * ecount) / (double)(n2 * (n2 - 1));
+    PeelBook bk(n2, kmax, I, *R, tot, e2);
     Rec rec;
     rec.kmax = (uint32_t)kmax;
     rec.core = std::max<uint32_t>(I.core, 1);
@@ -258,57 +391,90 @@ kclpp_status kclpp_trim(kclpp_ctx *ctx, const kclpp_edge_list *el, int kmax, int
     rec.merge.assign((size_t)(kmax - 2) * rec.core + 1, 0);
     rec.size.assign(kmax, 0);
     rec.ck.assign(kmax, 0);
-    rec.nck = nck2.data();
-    uint32_t i;
-    for (i = 0; i + 1 < n2; ++i) {
-      uint64_t v;
-      const uint32_t u = h.pop(&v);
-      if (v > c) c = v;
-      R->order[i] = u;
-      R->core_num[i] = c;
-      // oneshortpass (:577-603)
-      uint32_t s = 0;
-      for (uint64_t j = cu[u]; j < cu[u + 1]; ++j)
-        if (h.live(au[j])) live[s++] = au[j];
-      if (s > (uint32_t)kmax - 2) {
-        rec.ck[0] = u;
-        for (uint32_t q = 0; q < s; ++q) {
-          const uint32_t w = live[q];
-          rec.ck[1] = w;
-          rec.size[0] = isect(live.data(), s, adj.data() + cd[w], (uint32_t)(cd[w + 1] - cd[w]), rec.merge.data());
-          rec.run(3);
-        }
+    std::vector<uint64_t> nck2((size_t)n2 + 1, 0);
+    kclpp_peel_stats &PS = R->peel;
+    if (mode == KCLPP_TRIM_EXACT_HOST) {
+      std::vector<uint32_t> live((size_t)n2 + 1);
+      std::vector<uint64_t> W((size_t)n2 + 1);
+      while (bk.i + 1 < n2) {
+        uint64_t v;
+        const uint32_t u = h.pop(&v);
+        uint32_t na = 0;
+        for (uint64_t j = cu[u]; j < cu[u + 1]; ++j)
+          if (h.live(au[j])) live[na++] = au[j];
+        recount_host(rec, u, live.data(), na, nck2.data(), W.data());
+        bk.commit(h, u, v, live.data(), na, W.data());
+        PS.host_roots += na > (uint32_t)kmax - 2;
       }
-      uint64_t ncktot2 = 0;
-      for (uint64_t j = cu[u]; j < cu[u + 1]; ++j) {
-        const uint32_t w = au[j];
-        if (h.live(w)) {
-          ecount--;
-          h.dec(w, nck2[w]);
-          ncktot2 += nck2[w];
-          nck2[w] = 0;
+      PS.committed = PS.predicted = n2 ? n2 - 1 : 0;
+      PS.batches = PS.committed;
+    } else {
+      kclpp_graph *gd = nullptr;
+      kclpp_status st = kclpp_graph_from_csr(ctx, n2, e2, cd.data(), adj.data(), &gd);
+      if (st != KCLPP_OK) return st;
+      std::unique_ptr<kclpp_graph, void (*)(kclpp_graph *)> gd_own(gd, kclpp_graph_free);
+      PeelRecount *P = nullptr;
+      st = peel_recount_create(ctx, gd, kmax, &P);
+      if (st != KCLPP_OK) return st;
+      std::unique_ptr<PeelRecount, void (*)(PeelRecount *)> P_own(P, peel_recount_free);
+      HeapPeek peek(h);
+      std::vector<uint32_t> pred, mark((size_t)n2, 0), mpos((size_t)n2, 0), lcols;
+      std::vector<uint64_t> loff, W;
+      std::vector<uint8_t> gpu;
+      uint32_t gen = 0;
+      uint32_t B = 64;
+      constexpr uint32_t kMaxBatch = 4096;
+      while (bk.i + 1 < n2) {
+        const uint32_t want = std::min<uint32_t>(B, n2 - 1 - bk.i);
+        peek.reset();
+        if (++gen == 0) {
+          std::fill(mark.begin(), mark.end(), 0);
+          gen = 1;
         }
-      }
-      const uint32_t size_tmp = n2 - i - 1;
-      whendel[size_tmp] = ncktot2 / (uint64_t)(kmax - 1);
-      ncktot -= whendel[size_tmp];
-      const double ckrho_tmp = (double)ncktot / (double)size_tmp;
-      if (ckrho_tmp > I.ckrho) {
-        I.ckrho = ckrho_tmp;
-        I.size = size_tmp;
-        I.rho = (double)(2 * ecount) / (double)(size_tmp * (size_tmp - 1));
+        pred.resize(want);
+        for (uint32_t j = 0; j < want; ++j) {
+          pred[j] = peek.pop();
+          mark[pred[j]] = gen;
+          mpos[pred[j]] = j;
+        }
+        loff.assign((size_t)want + 1, 0);
+        lcols.clear();
+        gpu.assign(want, 0);
+        for (uint32_t j = 0; j < want; ++j) {
+          const uint32_t u = pred[j];
+          for (uint64_t q = cu[u]; q < cu[u + 1]; ++q) {
+            const uint32_t v = au[q];
+            if (h.live(v) && !(mark[v] == gen && mpos[v] < j)) lcols.push_back(v);
+          }
+          loff[j + 1] = lcols.size();
+          const uint64_t d = loff[j + 1] - loff[j];
+          gpu[j] = d > (uint64_t)kmax - 2 && d <= KCLPP_MAX_OUTDEG;
+        }
+        W.assign(lcols.size(), 0);
+        for (uint32_t j = 0; j < want; ++j) {
+          const uint64_t d = loff[j + 1] - loff[j];
+          if (d > KCLPP_MAX_OUTDEG) {  // beyond the GPU tiers: the host's recursion
+            recount_host(rec, pred[j], lcols.data() + loff[j], (uint32_t)d, nck2.data(), W.data() + loff[j]);
+            PS.host_roots++;
+          }
+        }
+        st = peel_recount_run(P, want, loff.data(), lcols.data(), gpu.data(), W.data());
+        if (st != KCLPP_OK) return st;
+        uint32_t j = 0;
+        for (; j < want && h.key[0] == pred[j]; ++j) {
+          uint64_t v;
+          const uint32_t u = h.pop(&v);
+          bk.commit(h, u, v, lcols.data() + loff[j], (uint32_t)(loff[j + 1] - loff[j]), W.data() + loff[j]);
+          PS.gpu_roots += gpu[j];
+        }
+        PS.batches++;
+        PS.predicted += want;
+        PS.committed += j;
+        B = j == want ? std::min(2 * B, kMaxBatch) : std::max<uint32_t>(1, 2 * j);
       }
     }
-    I.ntrim = n2;  // the reference leaves ntrim unset when n2 == 1
-    for (uint32_t j = n2 - 1; j >= 1; --j) {
-      if ((double)whendel[j] >= I.ckrho) { I.ntrim = j + 1; break; }
-      I.ncktrim -= whendel[j];
-    }
-    uint64_t v;
-    R->order[i] = h.pop(&v);
-    R->core_num[i] = c;
-    I.ckcore = c;
-    for (uint32_t q = n2 - 1; q != n2 - I.ntrim - 1; --q) alive[R->order[q]] = 1;
+    bk.finish(h, alive);
+    PS.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_peel).count();
   } else {
     // FAST: density-threshold rounds on the GPU.
     std::vector<uint64_t> nck = R->nck;
@@ -386,6 +552,12 @@ kclpp_status kclpp_trim_copy(const kclpp_trim_result *t, uint32_t *map, uint64_t
   if (nck && n2) memcpy(nck, t->nck.data(), n2 * 8);
   if (order && n2) memcpy(order, t->order.data(), n2 * 4);
   if (core_num && n2) memcpy(core_num, t->core_num.data(), n2 * 8);
+  return KCLPP_OK;
+}
+
+kclpp_status kclpp_trim_peel_stats(const kclpp_trim_result *t, kclpp_peel_stats *st) {
+  if (!t || !st) return set_error(KCLPP_ERR_INVALID, "null argument");
+  *st = t->peel;
   return KCLPP_OK;
 }
 

@@ -1302,3 +1302,91 @@ orc_sampling_info orc_sampling_extract(uint32_t n, int k, uint64_t S, const uint
   free(push);
   return info;
 }
+
+/* ---- the benchmark's input graph (see kclpp_oracle.h) ------------------- */
+typedef struct { uint64_t x; } orc_splitmix;
+static inline uint64_t sm_next(orc_splitmix *r) {
+  uint64_t z = (r->x += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static inline double sm_uniform(orc_splitmix *r) { return (double)(sm_next(r) >> 11) * (1.0 / 9007199254740992.0); }
+static inline uint64_t sm_below(orc_splitmix *r, uint64_t m) { return m ? sm_next(r) % m : 0; }
+static inline uint64_t orc_pack(uint32_t u, uint32_t v) {
+  if (u > v) { uint32_t t = u; u = v; v = t; }
+  return ((uint64_t)u << 32) | v;
+}
+
+static void radix_u64(uint64_t *k, uint64_t n) {
+  uint64_t *tmp = (uint64_t *)malloc((n ? n : 1) * sizeof(uint64_t));
+  size_t *cnt = (size_t *)malloc((1u << 16) * sizeof(size_t));
+  for (int sh = 0; sh < 64; sh += 16) {
+    memset(cnt, 0, (1u << 16) * sizeof(size_t));
+    for (uint64_t i = 0; i < n; ++i) cnt[(k[i] >> sh) & 0xFFFF]++;
+    size_t sum = 0;
+    for (uint32_t d = 0; d < (1u << 16); ++d) { size_t t = cnt[d]; cnt[d] = sum; sum += t; }
+    for (uint64_t i = 0; i < n; ++i) tmp[cnt[(k[i] >> sh) & 0xFFFF]++] = k[i];
+    memcpy(k, tmp, n * sizeof(uint64_t));
+  }
+  free(cnt);
+  free(tmp);
+}
+
+int orc_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+             uint32_t **pairs, uint64_t *e, uint32_t *n_out) {
+  if (scale < 1 || scale > 31 || edge_factor < 1) return -1;
+  orc_splitmix r = {seed * 0x2545F4914F6CDD1Dull + 0x1234567ull};
+  const double ab = a + b, abc = a + b + c;
+  const uint32_t n = 1u << scale;
+  const uint64_t samples = (uint64_t)edge_factor << scale;
+  uint64_t *keys = (uint64_t *)malloc(samples * sizeof(uint64_t));
+  uint64_t m = 0;
+  for (uint64_t i = 0; i < samples; ++i) {
+    uint32_t u = 0, v = 0;
+    for (uint32_t l = 0; l < scale; ++l) {
+      const double x = sm_uniform(&r);
+      uint32_t bu = 0, bv = 0;
+      if (x < a) {
+      } else if (x < ab) {
+        bv = 1;
+      } else if (x < abc) {
+        bu = 1;
+      } else {
+        bu = 1;
+        bv = 1;
+      }
+      u = (u << 1) | bu;
+      v = (v << 1) | bv;
+    }
+    if (u != v) keys[m++] = ((uint64_t)u << 32) | v;  /* ends mapped before canonicalising */
+  }
+  uint32_t *perm = (uint32_t *)malloc((size_t)n * sizeof(uint32_t));
+  for (uint32_t i = 0; i < n; ++i) perm[i] = i;
+  for (uint32_t i = n; i > 1; --i) {
+    const uint64_t j = sm_below(&r, i);
+    const uint32_t t = perm[i - 1];
+    perm[i - 1] = perm[j];
+    perm[j] = t;
+  }
+  for (uint64_t i = 0; i < m; ++i) keys[i] = orc_pack(perm[(uint32_t)(keys[i] >> 32)], perm[(uint32_t)keys[i]]);
+  free(perm);
+  radix_u64(keys, m);
+  uint64_t w = 0;
+  for (uint64_t i = 0; i < m; ++i)
+    if (w == 0 || keys[i] != keys[w - 1]) keys[w++] = keys[i];
+  uint32_t *P = (uint32_t *)malloc((w ? 2 * w : 2) * sizeof(uint32_t));
+  uint32_t mx = 0;
+  for (uint64_t i = 0; i < w; ++i) {
+    P[2 * i] = (uint32_t)(keys[i] >> 32);
+    P[2 * i + 1] = (uint32_t)keys[i];
+    if (P[2 * i + 1] > mx) mx = P[2 * i + 1];
+  }
+  free(keys);
+  *pairs = P;
+  *e = w;
+  *n_out = w ? mx + 1 : 1;
+  return 0;
+}
+
+void orc_free(void *p) { free(p); }

@@ -145,6 +145,20 @@ int orc_seq_main(const orc_graph *g, int k, uint32_t num_iter, int mode, int thr
 int orc_sim_main(const orc_graph *g, int k, uint32_t num_iter, int threads,
                  double *rho_out, orc_info *infos, int max_infos);
 
+/* ---- the benchmark's input graph ----------------------------------------
+ * The library's seeded RMAT generator (kclistpp_gb300/csrc/kclpp_gen.cpp,
+ * KCLPP_GEN_RMAT), restated so that the CPU legs build the benchmark workload
+ * without loading the library: a SplitMix64 stream seeded with
+ * seed * 0x2545F4914F6CDD1D + 0x1234567; per sample, `scale` quadrant draws
+ * (uniform = top 53 bits / 2^53; a, a+b, a+b+c thresholds), self loops
+ * dropped; then a Fisher-Yates permutation of the 2^scale ids (swap i-1 with
+ * below(i) = next() % i, i from n down to 2) applied to both ends; pairs
+ * canonicalised (min, max), sorted and deduplicated; n = max id + 1.
+ * *pairs is malloc'd (2 * *e entries); returns 0 on success. */
+int orc_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+             uint32_t **pairs, uint64_t *e, uint32_t *n);
+void orc_free(void *p);
+
 /* ---- timing helper for the CPU baseline -------------------------------- */
 double orc_wtime(void);
 int orc_max_threads(void);

@@ -107,6 +107,9 @@ def lib() -> C.CDLL:
             "orc_sort_by_r_f64": (None, [C.c_uint32, f64p, u32p]),
             "orc_trim": (C.c_int, [C.c_uint32, C.c_uint64, C.POINTER(OrcEdge), C.c_int, C.POINTER(OrcTrim)]),
             "orc_free_trim": (None, [C.POINTER(OrcTrim)]),
+            "orc_rmat": (C.c_int, [C.c_uint32, C.c_uint32, C.c_double, C.c_double, C.c_double, C.c_uint64,
+                                   C.POINTER(u32p), u64p, u32p]),
+            "orc_free": (None, [C.c_void_p]),
             "orc_seq_main": (C.c_int, [G, C.c_int, C.c_uint32, C.c_int, C.c_int, u64p, C.POINTER(OrcInfo), C.c_int]),
             "orc_sim_main": (C.c_int, [G, C.c_int, C.c_uint32, C.c_int, f64p, C.POINTER(OrcInfo), C.c_int]),
             "orc_seq_pass_waves": (C.c_int, [G, C.c_int, u64p, C.c_uint32, C.c_int]),
@@ -336,6 +339,23 @@ def trim(pairs: np.ndarray, k: int, n: int | None = None) -> dict:
                     .reshape(-1, 2).copy() if res.mtrim else np.zeros((0, 2), np.uint32)),
     }
     lib().orc_free_trim(C.byref(res))
+    return out
+
+
+def rmat(scale: int, edge_factor: int, a: float = 0.57, b: float = 0.19, c: float = 0.19,
+         seed: int = 1) -> np.ndarray:
+    """The library's seeded RMAT graph, restated (kclpp_oracle.h, orc_rmat):
+    canonical (u < v) pairs, sorted and deduplicated, as an (e, 2) array."""
+    P = C.POINTER(C.c_uint32)()
+    e = C.c_uint64()
+    n = C.c_uint32()
+    if lib().orc_rmat(scale, edge_factor, a, b, c, seed, C.byref(P), C.byref(e), C.byref(n)) != 0:
+        raise ValueError("oracle rmat: bad parameters")
+    try:
+        out = np.ctypeslib.as_array(P, shape=(2 * e.value,)).reshape(-1, 2).copy() if e.value else \
+            np.zeros((0, 2), np.uint32)
+    finally:
+        lib().orc_free(P)
     return out
 
 

@@ -464,3 +464,13 @@ def test_null_arguments_never_crash():
     test instead of the session."""
     r = subprocess.run([sys.executable, "-c", NULL_PROBE, ROOT], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (r.returncode, r.stdout[-500:], r.stderr[-500:])
+
+
+def test_oracle_rmat_is_the_library_generator():
+    """The CPU legs build the benchmark graph with the oracle's restatement of
+    the library's RMAT generator (so that they load no library code); it must
+    give the library's graph exactly."""
+    for scale, ef, seed, (a, b, c) in ((6, 4, 2, (0.57, 0.19, 0.19)), (12, 16, 5, (0.57, 0.19, 0.19)),
+                                       (13, 8, 9, (0.45, 0.15, 0.15))):
+        want = K.rmat(scale, ef, a, b, c, seed=seed).pairs()
+        assert np.array_equal(O.rmat(scale, ef, a, b, c, seed=seed), want), (scale, ef, seed)
