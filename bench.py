@@ -314,8 +314,9 @@ def cpu_sample(pairs: np.ndarray, k: int, modes: list[str], seconds: float, thre
 # ---------------------------------------------------------------------------
 def convergence(ctx, gap: float = 0.01, max_passes: int = 400) -> dict:
     """Wall time to a certified density gap on a held-out graph: the zero-start
-    Seq run (per-root-edge streams) against the learned warm start and the
-    wave-ordered passes.  The network is trained here on zero-start runs of
+    Seq run (per-root-edge streams) against the learned warm start, the
+    wave-ordered passes, the shared-load passes (KCLPP_SEQ_SHARED) and the
+    warm start with shared-load passes.  The network is trained here on zero-start runs of
     seeded graphs of the same families (planted Chung-Lu and RMAT with planted
     communities, k = 5); evaluation is on an RMAT scale-16 graph with planted
     communities that the training never saw.  Every pass is followed by the
@@ -334,7 +335,9 @@ def convergence(ctx, gap: float = 0.01, max_passes: int = 400) -> dict:
     train_s = time.perf_counter() - t0
     g = K.build_graph(ctx, K.rmat_planted(16, 16, 8, 100, 400, 0.5, seed=79))
     runs = {}
-    for label, kw in (("zero", {}), ("warm", {"model": model}), ("waves", {"det_mode": K.SEQ_WAVES})):
+    for label, kw in (("zero", {}), ("warm", {"model": model}), ("waves", {"det_mode": K.SEQ_WAVES}),
+                      ("shared", {"det_mode": K.SEQ_SHARED}),
+                      ("warm_shared", {"model": model, "det_mode": K.SEQ_SHARED})):
         runs[label] = W.time_to_gap(g, k, gap, max_passes, trace=True, **kw)
     D = runs["zero"]["density"]
     out = {"graph": {"kind": "rmat scale 16, edge factor 16, 8 planted G(n_c, 0.5), n_c in [100, 400]",
@@ -349,10 +352,11 @@ def convergence(ctx, gap: float = 0.01, max_passes: int = 400) -> dict:
     fin = lambda x: x if math.isfinite(x) else None  # noqa: E731
     for lb in runs:
         out[lb]["seconds_to_zero_density"] = fin(out[lb]["seconds_to_zero_density"])
-    out["speedup_certified"] = {lb: z / runs[lb]["seconds"] for lb in ("warm", "waves")}
+    others = [lb for lb in runs if lb != "zero"]
+    out["speedup_certified"] = {lb: z / runs[lb]["seconds"] for lb in others}
     out["speedup_to_zero_density"] = {lb: (z / out[lb]["seconds_to_zero_density"]
                                            if out[lb]["seconds_to_zero_density"] else None)
-                                      for lb in ("warm", "waves")}
+                                      for lb in others}
     g.close()
     return out
 

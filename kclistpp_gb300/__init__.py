@@ -39,6 +39,7 @@ ERR_INVALID, ERR_IO, ERR_NOMEM, ERR_CUDA, ERR_UNSUPPORTED, ERR_OVERFLOW, ERR_NOD
 MAX_K = 8
 SEQ_EDGE_STREAMS = 1
 SEQ_WAVES = 2
+SEQ_SHARED = 3  # shared load vector, not deterministic (invariants only)
 TRIM_EXACT, TRIM_FAST, TRIM_EXACT_HOST = 0, 1, 2
 ORDER_EXACT, ORDER_FAST = 0, 1
 SAMPLE_TARGET = 10_000_000  # the reference's CLIQUES_TO_SAMPLE

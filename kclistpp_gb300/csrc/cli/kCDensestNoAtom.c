@@ -11,7 +11,9 @@
  * KCLPP_ORDER=fast in the environment builds the DAG from the bin-sort core
  * order (same degeneracy and clique counts, other ties) instead of SortByCore;
  * KCLPP_DET=waves runs the passes in the wave ordering (KCLPP_SEQ_WAVES, fewer
- * passes to the same certified gap) instead of per-root-edge streams;
+ * passes to the same certified gap) instead of per-root-edge streams, and
+ * KCLPP_DET=shared on one shared load vector (KCLPP_SEQ_SHARED, fewer passes
+ * still; not deterministic);
  * KCLPP_TUNE=file keeps the autotuned launch schedule in that file (tuned and
  * written on the first run, loaded on the next ones; no result changes).
  */
@@ -83,8 +85,10 @@ int main(int argc, char **argv) {
   printf("Number of nodes (degree > 0) = %u\n", n);
   printf("Iterate over all cliques\n");
   uint64_t *r = (uint64_t *)calloc((size_t)n + 1, sizeof(uint64_t));
-  const char *det = getenv("KCLPP_DET");  /* "waves": KCLPP_SEQ_WAVES */
-  const int det_mode = det && !strcmp(det, "waves") ? KCLPP_SEQ_WAVES : KCLPP_SEQ_EDGE_STREAMS;
+  const char *det = getenv("KCLPP_DET");  /* "waves": KCLPP_SEQ_WAVES; "shared": KCLPP_SEQ_SHARED */
+  const int det_mode = det && !strcmp(det, "waves")    ? KCLPP_SEQ_WAVES
+                       : det && !strcmp(det, "shared") ? KCLPP_SEQ_SHARED
+                                                       : KCLPP_SEQ_EDGE_STREAMS;
   uint32_t done = 0;
   for (uint32_t T = 1; T <= num_iter; T <<= 1) {
     CHECK(kclpp_seq_passes(ctx, g, k, T - done, det_mode, r));

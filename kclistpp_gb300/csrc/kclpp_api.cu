@@ -436,6 +436,14 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
 }
 
 // ---- device-resident passes (enqueue only) ---------------------------------
+// KCLPP_SEQ_SHARED: top-level steps of a stream between two hand-backs of its
+// increments to the load vector.
+constexpr uint32_t kSharedFlushSteps = 16;
+
+static bool valid_seq_mode(int m) {
+  return m == KCLPP_SEQ_EDGE_STREAMS || m == KCLPP_SEQ_WAVES || m == KCLPP_SEQ_SHARED;
+}
+
 // One Seq pass from `in` into `out`.  KCLPP_SEQ_WAVES runs the waves in order,
 // each wave's root-edge streams starting from r after the previous waves; it
 // uses `in` as the second ping-pong buffer (its contents are not needed after
@@ -461,6 +469,12 @@ static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsi
   dev::PassArgs a{};
   a.r_in = in;
   a.out = out;
+  if (det_mode == KCLPP_SEQ_SHARED) {
+    // One load vector, read and added to in place by every stream.
+    a.r_in = out;
+    a.shared_loads = 1;
+    a.flush_steps = kSharedFlushSteps;
+  }
   return run_tiers(c, g, dev::MODE_SEQ, k, a);
 }
 
@@ -759,6 +773,10 @@ kclpp_status kclpp_count_cliques(kclpp_ctx *c, const kclpp_graph *gc, int k, uin
 // ---- Seq --------------------------------------------------------------------------
 static kclpp_status seq_passes_on(kclpp_ctx *c, kclpp_graph *g, int k, uint32_t passes, unsigned long long *r,
                                   int det_mode = KCLPP_SEQ_EDGE_STREAMS) {
+  if (det_mode == KCLPP_SEQ_SHARED) {  // in place
+    for (uint32_t p = 0; p < passes; ++p) KCL_TRY(seq_pass_dev(c, g, k, r, r, det_mode));
+    return KCLPP_OK;
+  }
   // Ping-pong between r and the workspace; end with the result in r.
   unsigned long long *in = r, *out = g->d_b;
   for (uint32_t p = 0; p < passes; ++p) {
@@ -774,8 +792,7 @@ kclpp_status kclpp_seq_passes_dev(kclpp_ctx *c, const kclpp_graph *gc, int k, ui
   if (!c || !gc || (!r_dev && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
   KCL_TRY(check_unsharded(gc, "kclpp_seq_passes_dev"));
   KCL_TRY(check_k(k, 3));
-  if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
-    return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  if (!valid_seq_mode(det_mode)) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
   KCL_TRY(set_device(c));
   return seq_passes_on(c, const_cast<kclpp_graph *>(gc), k, passes, (unsigned long long *)r_dev, det_mode);
 }
@@ -785,8 +802,7 @@ kclpp_status kclpp_seq_passes(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32
   if (!c || !gc || (!r && gc->dag.n)) return set_error(KCLPP_ERR_INVALID, "null argument");
   KCL_TRY(check_unsharded(gc, "kclpp_seq_passes"));
   KCL_TRY(check_k(k, 3));
-  if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
-    return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  if (!valid_seq_mode(det_mode)) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
   const size_t bytes = (size_t)g->dag.n * 8;
@@ -1512,8 +1528,7 @@ kclpp_status kclpp_seq_main(kclpp_ctx *c, const kclpp_graph *gc, int k, uint32_t
   if (!c || !gc) return set_error(KCLPP_ERR_INVALID, "null argument");
   KCL_TRY(check_unsharded(gc, "kclpp_seq_main"));
   KCL_TRY(check_k(k, 3));
-  if (det_mode != KCLPP_SEQ_EDGE_STREAMS && det_mode != KCLPP_SEQ_WAVES)
-    return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
+  if (!valid_seq_mode(det_mode)) return set_error(KCLPP_ERR_INVALID, "unknown det_mode %d", det_mode);
   KCL_TRY(set_device(c));
   kclpp_graph *g = const_cast<kclpp_graph *>(gc);
   const uint32_t n = g->dag.n;

@@ -189,8 +189,14 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
       tau = warp_sum(t);
     }
     if constexpr (MODE == MODE_SEQ) {
-      for (int i = lane; i < d; i += 32) sm.base[i] = a.r_in[sm.list[i]];
-      if (lane == 0) sm.base[d] = a.r_in[s];
+      // Shared loads: the root's values as the load vector holds them now.
+      if (a.shared_loads) {
+        for (int i = lane; i < d; i += 32) sm.base[i] = __ldcg(a.out + sm.list[i]);
+        if (lane == 0) sm.base[d] = __ldcg(a.out + s);
+      } else {
+        for (int i = lane; i < d; i += 32) sm.base[i] = a.r_in[sm.list[i]];
+        if (lane == 0) sm.base[d] = a.r_in[s];
+      }
     }
     for (int i = lane; i < kSMaxD; i += 32) sm.rows[i] = 0;
     __syncwarp();
@@ -238,15 +244,22 @@ __global__ void __launch_bounds__(kWarpsS * 32) tier_s_kernel(PassArgs a) {
         if (!C) continue;
         const int g0 = sm.base[j] < sm.base[d] ? j : d;  // kCDensestNoAtom.c:287
         seq64<K - 2>(C, g0, sm.rows, sm.base, dl);
-        // Close the stream: its increments fell on {s, t} ∪ C.
+        // Close the stream: its increments fell on {s, t} ∪ C (shared loads:
+        // straight to the load vector).
+        auto close = [&](int i) {
+          if (!dl[i]) return;
+          if (a.shared_loads) atomicAdd(a.out + (i < d ? sm.list[i] : s), (unsigned long long)dl[i]);
+          else atomicAdd(&sm.acc[i], (unsigned long long)dl[i]);
+          dl[i] = 0;
+        };
         unsigned long long it = C;
         while (it) {
           const int i = __ffsll((long long)it) - 1;
           it &= it - 1;
-          if (dl[i]) { atomicAdd(&sm.acc[i], (unsigned long long)dl[i]); dl[i] = 0; }
+          close(i);
         }
-        if (dl[j]) { atomicAdd(&sm.acc[j], (unsigned long long)dl[j]); dl[j] = 0; }
-        if (dl[d]) { atomicAdd(&sm.acc[d], (unsigned long long)dl[d]); dl[d] = 0; }
+        close(j);
+        close(d);
       }
       __syncwarp();
       for (int i = lane; i <= d; i += 32) {
@@ -532,6 +545,42 @@ struct Vals64 {
   }
 };
 
+// Shared loads (KCLPP_SEQ_SHARED): a vertex's current value is the pass's
+// one load vector, read from L2 at every access (other streams' flushed
+// increments included), plus this stream's own unflushed increments (a u32
+// per vertex, owned by lane v & 31 as in Vals64).  v indexes the root's list
+// (list[v]; v == d is the root s itself).
+struct ValsShared {
+  using T = unsigned long long;
+  unsigned long long *r;
+  const uint32_t *list;
+  uint32_t s;
+  int d;
+  uint32_t *dl;
+  __device__ __forceinline__ unsigned long long *slot(int v) const { return r + (v < d ? list[v] : s); }
+  __device__ __forceinline__ T get(int v, uint32_t &raw) const {
+    raw = dl[v];
+    return __ldcg(slot(v)) + raw;
+  }
+  __device__ __forceinline__ void bump(int v, uint32_t raw, uint32_t *err) const {
+    if (raw == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
+    dl[v] = raw + 1u;
+  }
+  __device__ __forceinline__ void add(int v, T delta, uint32_t *err) const {
+    const unsigned long long nd = (unsigned long long)dl[v] + delta;
+    if (nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
+    dl[v] = (uint32_t)nd;
+  }
+  // Hands vertex v's unflushed increments to the load vector (its owner lane).
+  __device__ __forceinline__ void flush(int v) const {
+    const uint32_t x = dl[v];
+    if (x) {
+      atomicAdd(slot(v), (unsigned long long)x);
+      dl[v] = 0;
+    }
+  }
+};
+
 // Distance from the prefix value c to a candidate's value, as the chain's
 // fixed point uses it: -1 below c, else the difference clamped to 2^31 - 1
 // (a plain 32-bit difference for Vals32, whose values all lie below 2^31).
@@ -762,6 +811,63 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
   }
 }
 
+// KCLPP_SEQ_SHARED: every root-edge stream of the current root against the
+// pass's one load vector r (in place).  The chain is the reference's
+// (kCDensestNoAtom.c:155-268) with each value read live: r plus the stream's
+// own increments not yet handed back; those are flushed to r with atomic adds
+// every flush_steps steps of the stream's top level and when it closes, and
+// the edge argmin's increments (kept in the chain's prefix value) at close.
+// Every clique still gives exactly one unit to one of its members, so r / T
+// stays a feasible load whatever the interleaving; which member gets it
+// depends on the timing of the other streams' flushes (not deterministic).
+template <int K, int WPL>
+__device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const uint32_t *rows, const uint32_t *list,
+                                                   uint32_t s, unsigned long long *r, uint32_t flush_steps,
+                                                   uint32_t *dl, int lane, uint32_t *err) {
+  const ValsShared va{r, list, s, d, dl};
+  for (;;) {
+    int q = 0;
+    if (lane == 0) q = (int)atomicAdd(next, 1u);
+    q = __shfl_sync(KCL_FULL, q, 0);
+    if (q >= d) break;
+    const int j = d - 1 - q;
+    const Bits<WPL> C = load_row<WPL, true>(rows, j, 0, lane);
+    if (!any_bits<WPL>(C)) continue;
+    for_members<WPL>(C, lane, [&](int i) { dl[i] = 0; });
+    const unsigned long long vj = lane == 0 ? __ldcg(va.slot(j)) : 0ull, vd = lane == 0 ? __ldcg(va.slot(d)) : 0ull;
+    const int g0 = __shfl_sync(KCL_FULL, vj < vd ? j : d, 0);  // kCDensestNoAtom.c:287
+    const unsigned long long c0 = __shfl_sync(KCL_FULL, vj < vd ? vj : vd, 0);
+    unsigned long long cg = c0;
+    if constexpr (K == 3) {
+      cg = chain_words<WPL, ValsShared, false>(C, c0, va, 0u, lane, err);
+    } else {
+      bool live = true;
+      if constexpr (K - 2 >= 3) live = warp_sum(popc_lane(C)) >= K - 2;
+      if (live) {
+        uint32_t steps = 0;
+        for_each_bit<WPL>(C, [&](int u) {
+          const unsigned long long vu = value_of<ValsShared>(u, va, lane);
+          const bool take = vu < cg;
+          const Bits<WPL> Q = band(C, load_row<WPL, true>(rows, u, 0, lane));
+          const unsigned long long a0 = take ? vu : cg;
+          const unsigned long long a1 = seq_rec<K - 3, WPL, ValsShared, false>(Q, a0, rows, va, 0u, lane, err);
+          if (take) {
+            if (lane == (u & 31)) va.add(u, a1 - a0, err);
+          } else {
+            cg = a1;
+          }
+          if (++steps == flush_steps) {
+            steps = 0;
+            for_members<WPL>(C, lane, [&](int i) { va.flush(i); });
+          }
+        });
+      }
+    }
+    for_members<WPL>(C, lane, [&](int i) { va.flush(i); });
+    if (lane == 0 && cg != c0) atomicAdd(va.slot(g0), cg - c0);
+  }
+}
+
 // Work stealing: once the root list is exhausted, an idle CTA joins a root
 // whose sub-tasks (root edges or rows) are not all taken, rebuilds that root's
 // G_s and takes sub-tasks from the same global counter.  Every CTA publishes
@@ -930,7 +1036,10 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
       __syncthreads();
     }
     if constexpr (MODE == MODE_SEQ) {
-      seq_streams<K, WPL>(next, d, rows, base, dl, acc, lane, a.err);
+      if (a.shared_loads)
+        seq_streams_shared<K, WPL>(next, d, rows, list, s, a.out, a.flush_steps, dl, lane, a.err);
+      else
+        seq_streams<K, WPL>(next, d, rows, base, dl, acc, lane, a.err);
       __syncthreads();
       for (int i = tid; i <= d; i += NW * 32) {
         const unsigned long long v = acc[i];

@@ -1,0 +1,78 @@
+"""KCLPP_SEQ_SHARED: Seq-kClist++ passes on one shared load vector.
+
+Its results depend on the timing of the streams' atomic hand-backs, so they
+are not compared bit for bit; what must hold on every run:
+
+* conservation: one pass adds exactly the number of k-cliques to r (every
+  clique gives one unit to one of its members), in every launch group (tiers
+  S, M and L) and for k = 3..6;
+* the certificate: r / T is a feasible load, so for graphs small enough to
+  know the optimum rho* exactly, every report of the run satisfies
+  density <= rho* <= ub;
+* what the mode is for: on a graph with planted dense communities it reaches
+  a certified 1 % gap in fewer passes than the per-root-edge streams.
+"""
+import numpy as np
+import pytest
+
+import kclistpp_gb300 as K
+from kclistpp_gb300 import warm as W
+from tests.test_certify import _cliques, _rho_star, _small_graphs
+
+pytestmark = pytest.mark.gpu
+
+
+def graphs():
+    return {
+        "cl_s": K.chung_lu(5000, 14.0, 2.3, seed=11).pairs(),                         # tier S only
+        "planted_m": K.planted(4000, 6.0, 2.2, 2, 300, 400, 0.5, seed=12).pairs(),    # tier M
+        "planted_l": K.planted(3000, 4.0, 2.2, 1, 1500, 1500, 0.55, seed=14).pairs(),  # tier L
+    }
+
+
+GRAPHS = graphs()
+CASES = [("cl_s", k) for k in (3, 4, 5, 6)] + [("planted_m", k) for k in (3, 4, 5)] + [("planted_l", 3),
+                                                                                      ("planted_l", 4)]
+
+
+@pytest.mark.parametrize("name,k", CASES)
+def test_every_clique_gives_one_unit(ctx, name, k):
+    g = K.build_graph(ctx, K.EdgeList.from_pairs(GRAPHS[name]))
+    total, _ = K.count_cliques(g, k)
+    rng = np.random.default_rng(7)
+    for r0 in (np.zeros(g.n, np.uint64), rng.integers(0, 1000, size=g.n, dtype=np.uint64)):
+        r = r0.copy()
+        for p in range(3):
+            before = r.copy()
+            r = K.seq_passes(g, k, 1, r, K.SEQ_SHARED)
+            assert np.all(r >= before)
+            assert int((r - before).sum()) == total, f"pass {p}: the increments do not sum to the clique count"
+    g.close()
+
+
+@pytest.mark.parametrize("i,k", [(i, k) for i in range(len(_small_graphs())) for k in (3, 4)])
+def test_reports_certify_the_optimum(ctx, i, k):
+    n, pairs = _small_graphs()[i]
+    masks = _cliques(n, pairs, k)
+    if len(masks) == 0:
+        pytest.skip("no k-clique")
+    num, den = _rho_star(n, masks)
+    g = K.build_graph(ctx, K.EdgeList.from_pairs(pairs))
+    infos, r = K.seq_main(g, k, 64, K.SEQ_SHARED)
+    assert int(r.sum()) == 64 * len(masks)
+    for info in infos:
+        assert info.density * den <= num * (1 + 1e-12)
+        assert info.ub * den >= num * (1 - 1e-12)
+    g.close()
+
+
+def test_fewer_passes_to_a_certified_gap(ctx):
+    g = K.build_graph(ctx, K.rmat_planted(13, 16, 4, 60, 150, 0.5, seed=79))
+    k = 5
+    streams = W.time_to_gap(g, k, 0.01, 300)
+    shared = W.time_to_gap(g, k, 0.01, 300, det_mode=K.SEQ_SHARED)
+    assert shared["reached"]
+    assert shared["passes"] * 2 <= streams["passes"], (shared["passes"], streams["passes"])
+    # the same densest subgraph is found
+    assert abs(shared["density"] - streams["density"]) <= 0.01 * streams["density"]
+    g.close()
