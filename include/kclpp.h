@@ -259,14 +259,16 @@ kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, uint64_t m, c
  * waves, so the upper bound converges in several times fewer passes than
  * with EDGE_STREAMS, at the cost of W ordered launches per pass. */
 #define KCLPP_SEQ_WAVES 2
-/* SHARED (not deterministic): every stream reads the pass's one load vector
- * live and hands its increments back with atomic adds every few steps and at
- * its end, so a clique sees most increments that other streams made before
- * it (closer to the reference's sequential p = 1 order than any ordering of
- * private streams).  Every clique still gives exactly one unit to one of its
- * members, so r / T stays a feasible load and the upper bound of
- * kCDensestNoAtom.c:352-369 stays a certificate; which member gets the unit
- * depends on timing, so r differs from run to run. */
+/* SHARED (not deterministic): the root-edge streams share the pass's one load
+ * vector, updated in place: a stream starts from the vector as the streams
+ * closed before it left it (and sees its CTA's other streams as they close),
+ * and adds its increments back when it closes.  Its cliques see far fresher
+ * loads than with EDGE_STREAMS (closer to the reference's sequential p = 1
+ * order), so the certified gap closes in several times fewer passes.  Every
+ * clique still gives exactly one unit to one of its members, so r / T stays
+ * a feasible load and the upper bound of kCDensestNoAtom.c:352-369 stays a
+ * certificate; which member gets the unit depends on timing, so r differs
+ * from run to run. */
 #define KCLPP_SEQ_SHARED 3
 /* `passes` FRANK_WOLFE passes (CDF_CliqueEnum, kCDensestNoAtom.c:270-295) on
  * r (n entries, u64 as in kCDensestNoAtom.c:124). */

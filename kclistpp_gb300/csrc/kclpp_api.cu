@@ -436,10 +436,6 @@ static kclpp_status run_tiers(kclpp_ctx *c, kclpp_graph *g, int mode, int k, dev
 }
 
 // ---- device-resident passes (enqueue only) ---------------------------------
-// KCLPP_SEQ_SHARED: top-level steps of a stream between two hand-backs of its
-// increments to the load vector.
-constexpr uint32_t kSharedFlushSteps = 16;
-
 static bool valid_seq_mode(int m) {
   return m == KCLPP_SEQ_EDGE_STREAMS || m == KCLPP_SEQ_WAVES || m == KCLPP_SEQ_SHARED;
 }
@@ -473,7 +469,6 @@ static kclpp_status seq_pass_dev(kclpp_ctx *c, kclpp_graph *g, int k, const unsi
     // One load vector, read and added to in place by every stream.
     a.r_in = out;
     a.shared_loads = 1;
-    a.flush_steps = kSharedFlushSteps;
   }
   return run_tiers(c, g, dev::MODE_SEQ, k, a);
 }

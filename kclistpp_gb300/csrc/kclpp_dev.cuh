@@ -63,11 +63,9 @@ struct PassArgs {
   const uint32_t *list_cols;
   unsigned long long *pair_out;
   // MODE_SEQ with shared loads (KCLPP_SEQ_SHARED): out is the one load vector
-  // of the pass, read live (from L2) by every stream and added to in place;
-  // a stream's own increments are flushed every flush_steps steps of its top
-  // level and when it closes.
+  // of the pass, read by every stream when it starts and added to in place
+  // when it closes.
   int shared_loads;
-  uint32_t flush_steps;
 };
 
 // A root's member list: its DAG out-list, or its explicit list (peel recounts).

@@ -545,22 +545,20 @@ struct Vals64 {
   }
 };
 
-// Shared loads (KCLPP_SEQ_SHARED): a vertex's current value is the pass's
-// one load vector, read from L2 at every access (other streams' flushed
-// increments included), plus this stream's own unflushed increments (a u32
-// per vertex, owned by lane v & 31 as in Vals64).  v indexes the root's list
-// (list[v]; v == d is the root s itself).
+// Shared loads (KCLPP_SEQ_SHARED): a vertex's current value is the root's
+// copy of the pass's one load vector (base, refreshed from it when a stream
+// starts) plus the increments the CTA's closed streams added (acc) plus this
+// stream's own (a u32 per vertex, owned by lane v & 31 as in Vals64).  Other
+// warps refresh and close concurrently, so a read is a recent snapshot: the
+// values steer which member gets a unit, never whether a unit is given.
 struct ValsShared {
   using T = unsigned long long;
-  unsigned long long *r;
-  const uint32_t *list;
-  uint32_t s;
-  int d;
+  const unsigned long long *base;
+  const unsigned long long *acc;
   uint32_t *dl;
-  __device__ __forceinline__ unsigned long long *slot(int v) const { return r + (v < d ? list[v] : s); }
   __device__ __forceinline__ T get(int v, uint32_t &raw) const {
     raw = dl[v];
-    return __ldcg(slot(v)) + raw;
+    return base[v] + *(const volatile unsigned long long *)(acc + v) + raw;
   }
   __device__ __forceinline__ void bump(int v, uint32_t raw, uint32_t *err) const {
     if (raw == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
@@ -570,14 +568,6 @@ struct ValsShared {
     const unsigned long long nd = (unsigned long long)dl[v] + delta;
     if (nd > 0xffffffffull) atomicOr(err, ERR_OVERFLOW);
     dl[v] = (uint32_t)nd;
-  }
-  // Hands vertex v's unflushed increments to the load vector (its owner lane).
-  __device__ __forceinline__ void flush(int v) const {
-    const uint32_t x = dl[v];
-    if (x) {
-      atomicAdd(slot(v), (unsigned long long)x);
-      dl[v] = 0;
-    }
   }
 };
 
@@ -812,19 +802,31 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
 }
 
 // KCLPP_SEQ_SHARED: every root-edge stream of the current root against the
-// pass's one load vector r (in place).  The chain is the reference's
-// (kCDensestNoAtom.c:155-268) with each value read live: r plus the stream's
-// own increments not yet handed back; those are flushed to r with atomic adds
-// every flush_steps steps of the stream's top level and when it closes, and
-// the edge argmin's increments (kept in the chain's prefix value) at close.
-// Every clique still gives exactly one unit to one of its members, so r / T
-// stays a feasible load whatever the interleaving; which member gets it
-// depends on the timing of the other streams' flushes (not deterministic).
+// pass's one load vector r (updated in place).  When a stream starts, the
+// CTA's copy of its vertices' values is refreshed from r (less what the CTA
+// itself already added, which acc holds); the chain is the reference's
+// (kCDensestNoAtom.c:155-268) on base + acc + the stream's own increments;
+// when it closes, its increments go to acc (seen at once by the CTA's other
+// streams) and, by atomic adds, to r (seen by every stream that starts
+// later).  Every clique still gives exactly one unit to one of its members,
+// so r / T stays a feasible load whatever the interleaving; which member
+// gets it depends on the timing of the other streams (not deterministic).
+// The vector is read and added to once per stream and vertex, not per
+// clique: the whole GPU reading a few kilobytes of L2 at every candidate
+// serialises on the few L2 slices that hold them.
 template <int K, int WPL>
 __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const uint32_t *rows, const uint32_t *list,
-                                                   uint32_t s, unsigned long long *r, uint32_t flush_steps,
-                                                   uint32_t *dl, int lane, uint32_t *err) {
-  const ValsShared va{r, list, s, d, dl};
+                                                   uint32_t s, unsigned long long *r, unsigned long long *base,
+                                                   unsigned long long *acc, uint32_t *dl, int lane, uint32_t *err) {
+  const ValsShared va{base, acc, dl};
+  auto id = [&](int i) { return i < d ? list[i] : s; };
+  auto refresh = [&](int i) {
+    base[i] = __ldcg(r + id(i)) - *(volatile unsigned long long *)(acc + i);
+  };
+  auto close = [&](int i, unsigned long long x) {
+    atomicAdd(acc + i, x);
+    atomicAdd(r + id(i), x);
+  };
   for (;;) {
     int q = 0;
     if (lane == 0) q = (int)atomicAdd(next, 1u);
@@ -833,38 +835,26 @@ __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const 
     const int j = d - 1 - q;
     const Bits<WPL> C = load_row<WPL, true>(rows, j, 0, lane);
     if (!any_bits<WPL>(C)) continue;
-    for_members<WPL>(C, lane, [&](int i) { dl[i] = 0; });
-    const unsigned long long vj = lane == 0 ? __ldcg(va.slot(j)) : 0ull, vd = lane == 0 ? __ldcg(va.slot(d)) : 0ull;
+    for_members<WPL>(C, lane, [&](int i) {
+      refresh(i);
+      dl[i] = 0;
+    });
+    unsigned long long vj = 0, vd = 0;
+    if (lane == 0) {
+      refresh(j);
+      refresh(d);
+      vj = base[j] + *(volatile unsigned long long *)(acc + j);
+      vd = base[d] + *(volatile unsigned long long *)(acc + d);
+    }
+    __syncwarp();
     const int g0 = __shfl_sync(KCL_FULL, vj < vd ? j : d, 0);  // kCDensestNoAtom.c:287
     const unsigned long long c0 = __shfl_sync(KCL_FULL, vj < vd ? vj : vd, 0);
-    unsigned long long cg = c0;
-    if constexpr (K == 3) {
-      cg = chain_words<WPL, ValsShared, false>(C, c0, va, 0u, lane, err);
-    } else {
-      bool live = true;
-      if constexpr (K - 2 >= 3) live = warp_sum(popc_lane(C)) >= K - 2;
-      if (live) {
-        uint32_t steps = 0;
-        for_each_bit<WPL>(C, [&](int u) {
-          const unsigned long long vu = value_of<ValsShared>(u, va, lane);
-          const bool take = vu < cg;
-          const Bits<WPL> Q = band(C, load_row<WPL, true>(rows, u, 0, lane));
-          const unsigned long long a0 = take ? vu : cg;
-          const unsigned long long a1 = seq_rec<K - 3, WPL, ValsShared, false>(Q, a0, rows, va, 0u, lane, err);
-          if (take) {
-            if (lane == (u & 31)) va.add(u, a1 - a0, err);
-          } else {
-            cg = a1;
-          }
-          if (++steps == flush_steps) {
-            steps = 0;
-            for_members<WPL>(C, lane, [&](int i) { va.flush(i); });
-          }
-        });
-      }
-    }
-    for_members<WPL>(C, lane, [&](int i) { va.flush(i); });
-    if (lane == 0 && cg != c0) atomicAdd(va.slot(g0), cg - c0);
+    const unsigned long long c1 = seq_rec<K - 2, WPL, ValsShared, false>(C, c0, rows, va, 0u, lane, err);
+    for_members<WPL>(C, lane, [&](int i) {
+      const uint32_t x = dl[i];
+      if (x) close(i, x);
+    });
+    if (lane == 0 && c1 != c0) close(g0, c1 - c0);
   }
 }
 
@@ -986,8 +976,13 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
       if (tid == 0) base[d] = vertex_key(a, s);
     }
     if constexpr (MODE == MODE_SEQ) {
-      for (int i = tid; i < d; i += NW * 32) base[i] = a.r_in[a.cols[o + i]];
-      if (tid == 0) base[d] = a.r_in[s];
+      if (a.shared_loads) {  // the load vector as it is now (from L2: other SMs add to it)
+        for (int i = tid; i < d; i += NW * 32) base[i] = __ldcg(a.out + a.cols[o + i]);
+        if (tid == 0) base[d] = __ldcg(a.out + s);
+      } else {
+        for (int i = tid; i < d; i += NW * 32) base[i] = a.r_in[a.cols[o + i]];
+        if (tid == 0) base[d] = a.r_in[s];
+      }
     }
     __syncthreads();
     if constexpr (MODE == MODE_ORDER) {
@@ -1037,14 +1032,15 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
     }
     if constexpr (MODE == MODE_SEQ) {
       if (a.shared_loads)
-        seq_streams_shared<K, WPL>(next, d, rows, list, s, a.out, a.flush_steps, dl, lane, a.err);
+        seq_streams_shared<K, WPL>(next, d, rows, list, s, a.out, base, acc, dl, lane, a.err);
       else
         seq_streams<K, WPL>(next, d, rows, base, dl, acc, lane, a.err);
       __syncthreads();
       for (int i = tid; i <= d; i += NW * 32) {
         const unsigned long long v = acc[i];
         if (v) {
-          atomicAdd(&a.out[i < d ? list[i] : s], v);
+          // shared loads: already in the load vector, stream by stream
+          if (!a.shared_loads) atomicAdd(&a.out[i < d ? list[i] : s], v);
           acc[i] = 0;
         }
       }
