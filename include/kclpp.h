@@ -315,6 +315,30 @@ typedef struct {
 } kclpp_exact_info;
 kclpp_status kclpp_densest_exact(const kclpp_edge_list *el, int k, kclpp_exact_info *info, uint8_t *members);
 
+/* The exact algorithm's certificate (kCDensestMem.c:329-432: PAVA, the
+ * stability check and the Goldberg-type integrality test), restated with
+ * per-vertex loads from GPU passes so that no clique is stored.  The candidate
+ * S is the first block of the isotonic regression of the prefix clique counts
+ * in the order of r (any Seq run's loads); then, in up to max_passes shared-
+ * load passes (KCLPP_SEQ_SHARED, doubling): "inside" holds when the loads of
+ * passes on G[S] alone show, by integer arithmetic, that no subset of S has a
+ * density above m / n; "outside" when passes on the graph with S's members out
+ * of reach give no vertex outside S more than m / n per pass.  Both together
+ * prove that S has the largest k-clique density of the graph, exactly m / n.
+ * members (n entries, or NULL) gets S's vertices. */
+typedef struct {
+  uint32_t n;              /* vertices of the candidate S                      */
+  uint64_t cliques;        /* its k-cliques m (density = m / n exactly)        */
+  double density;
+  int inside;              /* no subset of S is denser                         */
+  int outside;             /* no set with a vertex outside S is denser         */
+  int certified;           /* inside and outside: S is a densest subgraph      */
+  uint32_t passes_inside;  /* passes after which each condition held          */
+  uint32_t passes_outside;
+} kclpp_certify_info;
+kclpp_status kclpp_certify_densest(kclpp_ctx *ctx, const kclpp_graph *g, int k, const uint64_t *r,
+                                   uint32_t max_passes, kclpp_certify_info *info, uint32_t *members);
+
 /* ---- checkpoints (no reference counterpart: its dump of r is commented out,
  * kCDensestNoAtom.c:398-401).  Host only: a run's vector -- Seq r (u64) or
  * Sim rho (f64, by bit pattern) -- with the passes done, k and a hash of its

@@ -79,6 +79,15 @@ class PeelStats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class CertifyInfo(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("cliques", C.c_uint64), ("density", C.c_double), ("inside", C.c_int),
+                ("outside", C.c_int), ("certified", C.c_int), ("passes_inside", C.c_uint32),
+                ("passes_outside", C.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class StateInfo(C.Structure):
     _fields_ = [("kind", C.c_int), ("k", C.c_int), ("passes", C.c_uint32), ("n", C.c_uint32),
                 ("graph_hash", C.c_uint64)]
@@ -242,6 +251,7 @@ _SIGS = {
     "kclpp_trim_copy": (C.c_int, [_P, _u32p, _u64p, _u32p, _u64p]),
     "kclpp_trim_edges": (C.c_int, [_P, C.POINTER(_P)]),
     "kclpp_trim_peel_stats": (C.c_int, [_P, C.POINTER(PeelStats)]),
+    "kclpp_certify_densest": (C.c_int, [_P, _P, C.c_int, _u64p, C.c_uint32, C.POINTER(CertifyInfo), _u32p]),
     "kclpp_trim_free": (None, [_P]),
     "kclpp_sampling_create": (C.c_int, [_P, _P, C.c_int, C.c_uint64, C.c_uint64, C.c_uint32, C.POINTER(_P)]),
     "kclpp_sampling_info_get": (C.c_int, [_P, C.POINTER(SamplingInfo)]),
@@ -767,6 +777,17 @@ def load_state(path: str) -> tuple[StateInfo, np.ndarray]:
     v = np.empty(info.n, dtype=np.uint64 if info.kind == KERNEL_SEQ else np.float64)
     _check(_lib.kclpp_load_state(os.fsencode(path), C.byref(info), v.ctypes.data_as(_P), info.n))
     return info, v
+
+
+def certify_densest(g: Graph, k: int, r: np.ndarray, max_passes: int = 4096) -> tuple[CertifyInfo, np.ndarray]:
+    """Exact certificate of the densest prefix of r (kCDensestMem.c:329-432,
+    restated with GPU passes): (info, the candidate's vertices)."""
+    r = np.ascontiguousarray(r, dtype=np.uint64)
+    info = CertifyInfo()
+    mem = np.zeros(max(g.n, 1), dtype=np.uint32)
+    _check(_lib.kclpp_certify_densest(g.ctx.handle, g._h, k, _ptr(r, C.c_uint64), max_passes, C.byref(info),
+                                      _ptr(mem, C.c_uint32)))
+    return info, mem[: info.n].copy()
 
 
 def densest_exact(el: EdgeList, k: int) -> tuple[ExactInfo, np.ndarray]:

@@ -34,7 +34,8 @@ NVCCFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr"
                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE]
 
 CU_SOURCES = ["kclpp_api.cu", "kclpp_k_count.cu", "kclpp_k_order.cu", "kclpp_k_seq.cu", "kclpp_warm.cu", "kclpp_sample.cu", "kclpp_peel.cu"]
-CPP_SOURCES = ["kclpp_gen.cpp", "kclpp_order.cpp", "kclpp_trim.cpp", "kclpp_state.cpp", "kclpp_exact.cpp"]
+CPP_SOURCES = ["kclpp_gen.cpp", "kclpp_order.cpp", "kclpp_trim.cpp", "kclpp_state.cpp", "kclpp_exact.cpp",
+               "kclpp_certify.cpp"]
 PROGRAMS = ["kCDensestNoAtom", "kCDensestCmpSync", "kClistCoreTrim", "NormalGraphCoreTrim", "kCDensestSamplingKclistpp"]
 
 
