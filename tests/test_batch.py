@@ -1,11 +1,13 @@
 """Batched runs (many graphs, several k, one captured CUDA graph) and the
-schedule autotuner.  The oracle for a batch is each graph run on its own:
-every slice of the batch's result must equal the single-graph run bit for
-bit, and a tuned schedule must not change any result."""
+schedule autotuner.  Every slice of the batch's result must equal the
+single-graph run bit for bit (and, for k = 6, 7 of the batched
+configuration's shape, the oracle's passes), and a tuned schedule must not
+change any result."""
 import numpy as np
 import pytest
 
 import kclistpp_gb300 as K
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -78,6 +80,18 @@ def test_batch_of_config4_shape(ctx):
         g = K.build_graph(ctx, els[gi])
         for ki, k in enumerate(ks):
             assert np.array_equal(out[ki, b.slice(gi)], K.seq_passes(g, k, 4))
+    # k = 6, 7 slices against the oracle itself (the reference's chain, one
+    # stream per root edge), not only against the library's own single runs
+    threads = max(1, min(16, O.max_threads()))
+    for gi in (0, 7):
+        og = O.Graph(els[gi].pairs())
+        for ki, k in enumerate(ks):
+            if k < 6:
+                continue
+            r = np.zeros(og.n, np.uint64)
+            for _ in range(4):
+                r = og.seq_pass(k, r, O.SEQ_EDGE_STREAMS, threads)
+            assert np.array_equal(out[ki, b.slice(gi)], r), f"graph {gi} k={k}"
 
 
 def _knob_graph():
