@@ -857,6 +857,16 @@ def main() -> None:
         parity = parity_check(K, ctx, a, g, pairs, r_start, rho_start, t_start, el_full)
         parity["trim"] = meta.get("trim_matches_reference")
 
+    cert = None
+    if rank == 0 and world == 1 and not a.no_parity:
+        # The exact certificate of the densest prefix (kCDensestMem.c:329-467,
+        # restated with GPU passes), from the loads of 64 shared-load passes.
+        t0 = time.time()
+        _, r_c = K.seq_main(g, a.k, 64, K.SEQ_SHARED)
+        ci, _ = K.certify_densest(g, a.k, r_c, 128)
+        cert = {**ci.as_dict(), "seconds": round(time.time() - t0, 2),
+                "note": "inside needs loads uniform on S to 1/(n j) or a max-flow on G[S] (at most 2e7 k-cliques)"}
+
     conv = None
     if rank == 0 and world == 1 and not a.no_convergence:
         conv = convergence(ctx)
@@ -868,7 +878,7 @@ def main() -> None:
                 "vs_baseline": None, "dtype": "u64+f64", "data": "synthetic", "config": config,
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
                 "clocks": clk, "kernels": kernels, "step_ms": step_ms, "wall_s": wall, "parity": parity,
-                "convergence": conv}
+                "certificate": cert, "convergence": conv}
         print(json.dumps(line), flush=True)
     g.close()
     ctx.close()

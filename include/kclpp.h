@@ -325,12 +325,16 @@ kclpp_status kclpp_densest_exact(const kclpp_edge_list *el, int k, kclpp_exact_i
  * density above m / n; "outside" when passes on the graph with S's members out
  * of reach give no vertex outside S more than m / n per pass.  Both together
  * prove that S has the largest k-clique density of the graph, exactly m / n.
+ * Where the loads do not settle "inside" within max_passes and G[S] has at
+ * most 2e7 k-cliques, the host max-flow (kclpp_densest_exact) on G[S] decides
+ * it, as the reference falls back to its max-flow (kCDensestMem.c:434-467).
  * members (n entries, or NULL) gets S's vertices. */
 typedef struct {
   uint32_t n;              /* vertices of the candidate S                      */
   uint64_t cliques;        /* its k-cliques m (density = m / n exactly)        */
   double density;
   int inside;              /* no subset of S is denser                         */
+  int inside_method;       /* 1: by the loads; 2: by max-flow on G[S]          */
   int outside;             /* no set with a vertex outside S is denser         */
   int certified;           /* inside and outside: S is a densest subgraph      */
   uint32_t passes_inside;  /* passes after which each condition held          */

@@ -81,7 +81,8 @@ class PeelStats(C.Structure):
 
 class CertifyInfo(C.Structure):
     _fields_ = [("n", C.c_uint32), ("cliques", C.c_uint64), ("density", C.c_double), ("inside", C.c_int),
-                ("outside", C.c_int), ("certified", C.c_int), ("passes_inside", C.c_uint32),
+                ("inside_method", C.c_int), ("outside", C.c_int), ("certified", C.c_int),
+                ("passes_inside", C.c_uint32),
                 ("passes_outside", C.c_uint32)]
 
     def as_dict(self):

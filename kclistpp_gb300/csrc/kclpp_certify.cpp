@@ -19,6 +19,10 @@
 //            every j either C(j, k) < c_min(j) or the top-j load sum is below
 //            c_min(j) T, no subset of S is denser than S (integer arithmetic,
 //            no tolerance).
+//            The margin can be as small as 1 / (n j), which the loads reach only
+//            after very many passes; where G[S] is small enough, the library's
+//            max-flow (kclpp_densest_exact) decides it exactly instead, as the
+//            reference falls back to its max-flow (:434-467).
 //   outside: loads b_out from Seq passes on G in which the members of S start
 //            at a value no clique can bring the others up to, so every clique
 //            with a member outside S gives its unit outside S.  Any X = A u Y
@@ -48,6 +52,10 @@ using namespace kclpp;
 namespace {
 
 typedef unsigned __int128 u128;
+
+// Largest G[S] (in k-cliques) handed to the host max-flow when the loads do
+// not settle "inside" (kclpp_densest_exact's own limit is 2e7).
+constexpr uint64_t kMaxFlowCliques = 20000000;
 
 // C(j, k), saturated at 2^64.
 u128 choose_capped(uint64_t j, int k) {
@@ -185,6 +193,21 @@ kclpp_status kclpp_certify_densest(kclpp_ctx *ctx, const kclpp_graph *g, int k, 
       }
     }
     if (inside && outside) break;
+  }
+  if (inside) info->inside_method = 1;
+  // The loads decide "inside" only once they are nearly uniform on S (the
+  // integrality margin can be 1 / (n j)); like the reference, which falls back
+  // to a max-flow when its Goldberg test fails (kCDensestMem.c:434-467), G[S]
+  // is then solved exactly where it is small enough: S's own density is the
+  // optimum of G[S] exactly when no subset of S is denser.
+  if (!inside && m <= kMaxFlowCliques) {
+    kclpp_exact_info ex;
+    const kclpp_status st = kclpp_densest_exact(el.get(), k, &ex, nullptr);
+    if (st != KCLPP_OK && st != KCLPP_ERR_UNSUPPORTED) return st;
+    if (st == KCLPP_OK && (u128)ex.num * ns == (u128)ex.den * m) {
+      inside = true;
+      info->inside_method = 2;
+    }
   }
   info->inside = inside;
   info->outside = outside;

@@ -27,7 +27,7 @@ def test_certificate_on_exhaustive_optimum(ctx, i, k):
     g = K.build_graph(ctx, K.EdgeList.from_pairs(pairs))
     _, r = K.seq_main(g, k, 64)
     info, mem = K.certify_densest(g, k, r, 1 << 14)
-    assert info.certified, info.as_dict()
+    assert info.certified and info.inside_method == 1, info.as_dict()  # the loads alone decide
     assert info.cliques * den == num * info.n  # exactly the optimum
     g.close()
 
@@ -49,7 +49,7 @@ def test_certificate_matches_max_flow(ctx, name, k):
     ex, _ = K.densest_exact(el, k)
     g = K.build_graph(ctx, el)
     _, r = K.seq_main(g, k, 64, K.SEQ_SHARED)
-    info, mem = K.certify_densest(g, k, r, 1 << 12)
+    info, mem = K.certify_densest(g, k, r, 256)
     assert info.certified, info.as_dict()
     assert info.cliques * ex.den == ex.num * info.n
     g.close()
