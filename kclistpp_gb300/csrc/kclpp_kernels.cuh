@@ -601,7 +601,7 @@ __device__ __forceinline__ int distance(T av, T c) {
 // by one scan and skipped.
 template <int WPL, typename VA, bool SKIP>
 __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typename VA::T c, const VA &va,
-                                                      uint32_t lo, int lane, uint32_t *err) {
+                                                      typename VA::T lo, int lane, uint32_t *err) {
   using T = typename VA::T;
   const uint32_t lt = lanemask_lt();
   uint32_t skip_mask = 0;
@@ -620,7 +620,7 @@ __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typena
       const uint32_t t = __shfl_up_sync(KCL_FULL, incl, o);
       if (lane >= o) incl += t;
     }
-    const bool ok = pop == 0 || lo >= (uint32_t)c + (incl - 1);
+    const bool ok = pop == 0 || lo >= c + (T)(incl - 1);
     const uint32_t bad = __ballot_sync(KCL_FULL, !ok);
     const int fb = bad ? __ffs(bad) - 1 : 32;
     if (fb > 0) {
@@ -675,7 +675,7 @@ __device__ __forceinline__ typename VA::T value_of(int x, const VA &va, int lane
 // written back by u's lane.
 template <int L, int WPL, typename VA, bool SKIP>
 __device__ __forceinline__ typename VA::T seq_rec(const Bits<WPL> &P, typename VA::T cg, const uint32_t *rows,
-                                                  const VA &va, uint32_t lo, int lane, uint32_t *err) {
+                                                  const VA &va, typename VA::T lo, int lane, uint32_t *err) {
   using T = typename VA::T;
   if constexpr (L == 1) {
     return chain_words<WPL, VA, SKIP>(P, cg, va, lo, lane, err);
@@ -835,10 +835,30 @@ __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const 
     const int j = d - 1 - q;
     const Bits<WPL> C = load_row<WPL, true>(rows, j, 0, lane);
     if (!any_bits<WPL>(C)) continue;
-    for_members<WPL>(C, lane, [&](int i) {
-      refresh(i);
-      dl[i] = 0;
-    });
+    // Refresh the members' values and take, per word of C (lane = word), the
+    // smallest of them: values only grow while the stream runs (up to the
+    // races of concurrent refreshes, which change which member gets a unit,
+    // never whether one is given), so a word whose candidates all start at or
+    // above the prefix's reach falls to the prefix whole (the chain's skip).
+    unsigned long long lo = ~0ull;
+#pragma unroll
+    for (int qq = 0; qq < WPL; ++qq) {
+      uint32_t nz = __ballot_sync(KCL_FULL, C.w[qq] != 0);
+      while (nz) {
+        const int L = __ffs(nz) - 1;
+        nz &= nz - 1;
+        const uint32_t word = __shfl_sync(KCL_FULL, C.w[qq], L);
+        unsigned long long val = ~0ull;
+        if ((word >> lane) & 1u) {
+          const int i = ((L + 32 * qq) << 5) | lane;
+          refresh(i);
+          dl[i] = 0;
+          val = base[i] + *(volatile unsigned long long *)(acc + i);
+        }
+        val = warp_min_u64(val);
+        if (qq == 0 && lane == L) lo = val;
+      }
+    }
     unsigned long long vj = 0, vd = 0;
     if (lane == 0) {
       refresh(j);
@@ -849,7 +869,7 @@ __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const 
     __syncwarp();
     const int g0 = __shfl_sync(KCL_FULL, vj < vd ? j : d, 0);  // kCDensestNoAtom.c:287
     const unsigned long long c0 = __shfl_sync(KCL_FULL, vj < vd ? vj : vd, 0);
-    const unsigned long long c1 = seq_rec<K - 2, WPL, ValsShared, false>(C, c0, rows, va, 0u, lane, err);
+    const unsigned long long c1 = seq_rec<K - 2, WPL, ValsShared, (WPL == 1)>(C, c0, rows, va, lo, lane, err);
     for_members<WPL>(C, lane, [&](int i) {
       const uint32_t x = dl[i];
       if (x) close(i, x);

@@ -59,11 +59,12 @@ def test_a_sparse_candidate_is_not_certified(ctx):
     """Loads that put a sparse path first make the first PAVA block a set that
     is not densest; the certificate must refuse it."""
     pairs = [(u, v) for u in range(8) for v in range(u + 1, 8)]  # K_8: 56 triangles, density 7
-    pairs += [(7 + i, 8 + i) for i in range(40)]                  # a path hanging on it
-    pairs += [(20, 60), (21, 60)]                                  # a triangle on the path
+    pairs += [(7 + i, 8 + i) for i in range(40)]                  # a path hanging on it (8..47)
+    pairs += [(20, 48), (21, 48)]                                  # a triangle on the path
     el = K.EdgeList.from_pairs(np.array(pairs, dtype=np.uint32))
     g = K.build_graph(ctx, el)
     rank = K.core_order(el)  # the DAG's vertex ids are the core ranks
+    assert g.n == el.n  # no isolated vertex
     r = np.zeros(g.n, np.uint64)
     for v in range(8, g.n):
         r[rank[v]] = 1000 + v
