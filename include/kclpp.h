@@ -209,7 +209,8 @@ kclpp_status kclpp_schedule_load(const char *path, uint64_t graph_hash, int k, i
 typedef struct kclpp_batch kclpp_batch;
 kclpp_status kclpp_batch_create(kclpp_ctx *ctx, const kclpp_edge_list *const *els, uint32_t count,
                                 kclpp_batch **out);
-/* union_graph (borrowed, may be NULL) can be tuned with kclpp_autotune. */
+/* union_graph (borrowed, may be NULL) can be tuned with kclpp_autotune; the
+ * next kclpp_batch_run then captures its graph again with the new schedule. */
 kclpp_status kclpp_batch_info(const kclpp_batch *b, uint32_t *graphs, uint32_t *total_n, uint64_t *total_m,
                               kclpp_graph **union_graph);
 /* offsets[i] = first union vertex of graph i (graphs + 1 entries). */

@@ -1149,6 +1149,7 @@ struct kclpp_batch {
   int exec_kernel = -1;
   std::vector<int> exec_ks;
   uint32_t exec_passes = 0;
+  kclpp_schedule exec_sched{};  // the union graph's schedule when the graph was captured
 };
 
 static void batch_release(kclpp_batch *b) {
@@ -1277,7 +1278,10 @@ kclpp_status kclpp_batch_run(kclpp_ctx *c, kclpp_batch *b, int kernel, const int
   const uint32_t n = g->dag.n;
   if (!n) return KCLPP_OK;
   const std::vector<int> want(ks, ks + nk);
-  const bool same = b->exec && b->exec_kernel == kernel && b->exec_ks == want && b->exec_passes == passes;
+  // A schedule set on the union graph since the capture (kclpp_autotune,
+  // kclpp_graph_set_schedule) changes the launches: capture again.
+  const bool same = b->exec && b->exec_kernel == kernel && b->exec_ks == want && b->exec_passes == passes &&
+                    memcmp(&b->exec_sched, &g->sp, sizeof g->sp) == 0;
   if (!same) {
     batch_release(b);
     if (!b->fork) KCL_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
@@ -1308,6 +1312,7 @@ kclpp_status kclpp_batch_run(kclpp_ctx *c, kclpp_batch *b, int kernel, const int
     b->exec_kernel = kernel;
     b->exec_ks = want;
     b->exec_passes = passes;
+    b->exec_sched = g->sp;
   }
   KCL_CUDA(cudaGraphLaunch(b->exec, c->stream));
   c->launches++;

@@ -128,3 +128,17 @@ def test_schedule_knobs_change_no_result(ctx):
         for k, (r_want, c_want) in want.items():
             assert np.array_equal(K.seq_passes(g, k, 2, r0), r_want), (cb, k)
             assert np.array_equal(K.sim_counts(g, k, rho0), c_want), (cb, k)
+
+
+def test_batch_tuned_schedule_keeps_results(ctx):
+    """Tuning the union graph after a run makes the next run capture its CUDA
+    graph again with the new schedule; the results stay the single runs'."""
+    els = _graphs()[:3]
+    b = K.Batch(ctx, els)
+    ks = [4, 6]
+    before = b.run(K.KERNEL_SEQ, ks, 2)
+    res = K.autotune(b.union_graph(), 6, K.KERNEL_SEQ)
+    assert res.candidates > 1
+    after = b.run(K.KERNEL_SEQ, ks, 2)
+    assert np.array_equal(before, after)
+    b.close()
