@@ -643,14 +643,18 @@ __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typena
       // Fixed point from "every candidate at or above c falls": once the
       // loads have spread, that guess is already exact and one vote confirms
       // it; ties (the first pass) take a few more rounds.
+      // (When no candidate is at or above c, every one takes its clique and
+      // the guess is the fixed point already: the second vote is skipped.)
       uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
-      uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
-      if (m2 != m) {
-        m = m2;
-        for (int r = 0; r < 32; ++r) {
-          m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
-          if (m2 == m) break;
+      if (m) {
+        uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+        if (m2 != m) {
           m = m2;
+          for (int r = 0; r < 32; ++r) {
+            m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+            if (m2 == m) break;
+            m = m2;
+          }
         }
       }
       if (valid && !((m >> lane) & 1u)) va.bump(v, raw, err);
