@@ -168,7 +168,8 @@ typedef struct {
   int steal_count;          /* work stealing in the counting kernels                              */
   uint32_t seq_waves;       /* waves of KCLPP_SEQ_WAVES, 1..1024 (default 4)                      */
   uint32_t seq_warps[4];    /* Seq kernel, warps per CTA of the M1 (<= seq_split1), M2 (<= split2), */
-                            /* M3 (<= 1024) and L root groups: 8, 12, 16, 20 or 24; 0 = the width  */
+                            /* M3 (<= 1024) and L root groups: 2, 4, 8, 12, 16, 20 or 24 (2 and 4:  */
+                            /* many small CTAs, for groups of small roots); 0 = the width of 8..24 */
                             /* that keeps the most warps resident per SM                           */
   int concurrent_tiers;     /* Seq kernel: launch a pass's root groups on forked streams (def. 1)  */
   uint32_t count_warps[4];  /* the counting / Sim kernels' widths of the same four groups:         */

@@ -926,8 +926,8 @@ kclpp_status kclpp_sim_update_dev(kclpp_ctx *c, uint32_t n, uint32_t t, double *
 static kclpp_status check_schedule(const kclpp_schedule *sp) {
   for (int i = 0; i < 4; ++i) {
     const uint32_t w = sp->seq_warps[i];
-    if (w != 0 && (w < 8 || w > (uint32_t)kWarpsMSeqMax || w % 4))
-      return set_error(KCLPP_ERR_INVALID, "seq_warps entries must be 0 or one of 8, 12, 16, 20, 24");
+    if (w != 0 && w != 2 && (w < 4 || w > (uint32_t)kWarpsMSeqMax || w % 4))
+      return set_error(KCLPP_ERR_INVALID, "seq_warps entries must be 0 or one of 2, 4, 8, 12, 16, 20, 24");
     const uint32_t v = sp->count_warps[i];
     if (v != 0 && (v < 8 || v > (uint32_t)kWarpsMMax || v % 8))
       return set_error(KCLPP_ERR_INVALID, "count_warps entries must be 0 or one of 8, 16, 24, 32");
@@ -1078,9 +1078,9 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
     // Warps per CTA, chosen per root group: the groups run as separate
     // launches, so each one's width is tuned on its own launch time.
     const bool sq = mode == dev::MODE_SEQ;
-    const uint32_t seq_w[5] = {8, 12, 16, 20, 24}, cnt_w[4] = {8, 16, 24, 32};
+    const uint32_t seq_w[7] = {2, 4, 8, 12, 16, 20, 24}, cnt_w[4] = {8, 16, 24, 32};
     const uint32_t *widths = sq ? seq_w : cnt_w;
-    const int nwid = sq ? 5 : 4;
+    const int nwid = sq ? 7 : 4;
     float bt[4] = {1e30f, 1e30f, 1e30f, 1e30f};
     kclpp_schedule tuned = best_sp;
     bool any = false;
@@ -1123,7 +1123,7 @@ kclpp_status kclpp_autotune(kclpp_ctx *c, kclpp_graph *g, int k, int kernel, kcl
   out->best = best_sp;
   out->best_ms = best;
   out->default_ms = def;
-  out->candidates = (int)cand.size() + 2 + (mode == dev::MODE_SEQ ? 6 : 5);
+  out->candidates = (int)cand.size() + 2 + (mode == dev::MODE_SEQ ? 8 : 5);
   return KCLPP_OK;
 }
 

@@ -1180,12 +1180,14 @@ static cudaError_t prepare(Fn fn, LaunchCache &lc, int threads, size_t smem, int
 
 // Warps per CTA of a tier M / L launch: `req` when nonzero, else the width
 // that keeps the most warps resident per SM at this out-degree bound (ties:
-// the narrower, i.e. more CTAs).  Seq: 8..24 in steps of 4; the counting
-// kernels: 8..32 in steps of 8.
+// the narrower, i.e. more CTAs).  Seq: 8..24 in steps of 4, and on request 2
+// or 4 (many small CTAs for groups of small roots, where a root has few root
+// edges to share out); the counting kernels: 8..32 in steps of 8.
 template <int MODE, int K, typename Fn>
 static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_in_smem, int req, int *nw) {
   using namespace dev;
-  constexpr int lo = 8, hi = warps_m<MODE, K>(), step = MODE == MODE_SEQ ? 4 : 8;
+  constexpr int hi = warps_m<MODE, K>(), step = MODE == MODE_SEQ ? 4 : 8;
+  const int lo = (MODE == MODE_SEQ && (req == 2 || req == 4)) ? req : 8;
   const int dev = current_device();
   {
     std::lock_guard<std::mutex> g(lc.mu);
@@ -1196,7 +1198,7 @@ static cudaError_t pick_warps(Fn fn, LaunchCache &lc, uint32_t dmax, bool rows_i
       }
   }
   int best = 0, best_warps = -1;
-  for (int w = lo; w <= hi; w += step) {
+  for (int w = lo; w <= hi; w = w < 8 ? w * 2 : w + step) {
     if (req > 0 && w != req) continue;
     const size_t sm = layout_m(MODE, K, dmax, w, rows_in_smem).total;
     if (sm > 227 * 1024) continue;

@@ -121,7 +121,8 @@ def test_schedule_knobs_change_no_result(ctx):
                    count_warps=[cw] * 4, tier_s_max=ts, tier_s_max_seq=tq, seq_split1=a, seq_split2=b,
                    m_split1=a, m_split2=b)
               for s, c, w, cw, ts, tq, a, b in [(0, 0, 8, 8, 64, 8, 128, 256), (1, 1, 24, 32, 32, 32, 256, 512),
-                                                (1, 0, 16, 16, 64, 16, 384, 768), (0, 1, 20, 24, 16, 64, 512, 1024)]]
+                                                (1, 0, 16, 16, 64, 16, 384, 768), (0, 1, 20, 24, 16, 64, 512, 1024),
+                                                (1, 1, 2, 8, 64, 8, 128, 256), (0, 0, 4, 16, 32, 16, 256, 512)]]
     for cb in combos:
         sp = K.Schedule(**{**base.as_dict(), **cb})
         K.set_schedule(g, sp)
