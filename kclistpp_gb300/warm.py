@@ -118,10 +118,19 @@ class WarmModel:
         self.close()
 
 
+# Passes' worth of predicted load a warm start begins with.  The upper bound
+# uses only the loads the run's own passes add, which first have to correct
+# the prediction's error, so a start worth many passes delays the certificate
+# (t0 = 16: 1.6x slower than the zero start on held-out RMAT-16 graphs); one
+# or two passes' worth breaks the first passes' ties by the prediction and
+# costs little (t0 = 2: 1.4-1.9x fewer passes there, measured over t0 = 1..16).
+DEFAULT_T0 = 2.0
+
+
 def time_to_gap(g: Graph, k: int, gap: float = 0.01, max_passes: int = 512, model: WarmModel | None = None,
-                t0: float = 16.0, trace: bool = False, det_mode: int = SEQ_EDGE_STREAMS) -> dict:
-    """Run Seq passes (per-root-edge streams, or waves with det_mode=SEQ_WAVES)
-    until (ub - density) / ub <= gap.
+                t0: float = DEFAULT_T0, trace: bool = False, det_mode: int = SEQ_EDGE_STREAMS) -> dict:
+    """Run Seq passes (per-root-edge streams; waves with det_mode=SEQ_WAVES;
+    shared loads with det_mode=SEQ_SHARED) until (ub - density) / ub <= gap.
 
     Zero start when model is None; otherwise start at r0 = model.start_r(g, t0)
     (the features, the inference and r0 are inside the timed region).  With

@@ -1,6 +1,6 @@
 """Learned warm start: the library's MLP kernels against an FP64 restatement,
 training on the method's own r vectors, and what the trained network gains
-over the plain zero-start run (passes to a certified 1% density gap)."""
+over the plain zero-start run (passes to a certified 1 % density gap)."""
 import numpy as np
 import pytest
 
@@ -57,15 +57,14 @@ def _community_graph(seed, n=6000):
 
 
 def test_warm_start_gain(ctx):
-    """Train on zero-start runs of seeded planted-community graphs (k = 5) and
-    evaluate on larger held-out graphs of the same kind.
-
-    What the network gains: the densest prefix (the lower bound) reaches 99.9%
-    of the best density found in fewer passes than the zero-start run.  What it
-    does not change: the certified gap, which needs an upper bound from a
-    feasible load -- the warm run's own increments -- and those converge at the
-    same rate from any start; both runs must stay certified (upper bound >=
-    every density either run found)."""
+    """What the trained network gains on the spec quantity, passes to a
+    certified 1 % density gap (the upper bound from the loads the run's own
+    passes added), on held-out RMAT graphs with planted communities (k = 5):
+    with the per-root-edge streams, fewer passes than the zero start; with
+    shared loads, under a third of the zero-start streams' passes.  Both
+    certificates stay valid (upper bound >= every density either run found).
+    (On planted Chung-Lu graphs the shared loads alone reach the gap in under
+    a tenth of the streams' passes and the warm start adds nothing there.)"""
     torch = pytest.importorskip("torch")
     from kclistpp_gb300 import warm as W
 
@@ -74,18 +73,23 @@ def test_warm_start_gain(ctx):
     X, Y = W.training_set(ctx, train, k, passes=64)
     m = W.WarmModel(ctx, seed=5)
     m.train(X, Y, steps=600, lr=1e-2)
-    zero_lb = warm_lb = 0
-    for el in (K.planted(60000, 10.0, 2.1, 10, 100, 400, 0.5, seed=77),
-               K.planted(65536, 12.0, 2.1, 6, 150, 500, 0.5, seed=78)):
+    zero = warm = warm_shared = 0
+    for el in (K.rmat_planted(16, 16, 8, 100, 400, 0.5, seed=79),
+               K.rmat_planted(16, 16, 8, 100, 400, 0.5, seed=80)):
         g = K.build_graph(ctx, el)
         z = W.time_to_gap(g, k, 0.01, 300, trace=True)
-        w = W.time_to_gap(g, k, 0.01, 300, model=m, t0=16.0, trace=True)
-        assert z["reached"] and w["reached"]
-        best = max(max(d for _, d, _ in z["trace"]), max(d for _, d, _ in w["trace"]))
-        assert w["ub"] >= best * (1 - 1e-12) and z["ub"] >= best * (1 - 1e-12)
-        zero_lb += W.passes_to_density(z["trace"], 0.999 * best)[0]
-        warm_lb += W.passes_to_density(w["trace"], 0.999 * best)[0]
-    assert 2 * warm_lb <= zero_lb, (warm_lb, zero_lb)
+        w = W.time_to_gap(g, k, 0.01, 300, model=m, trace=True)
+        ws = W.time_to_gap(g, k, 0.01, 300, model=m, trace=True, det_mode=K.SEQ_SHARED)
+        assert z["reached"] and w["reached"] and ws["reached"]
+        best = max(max(d for _, d, _ in r["trace"]) for r in (z, w, ws))
+        for r in (z, w, ws):
+            assert r["ub"] >= best * (1 - 1e-12)
+        zero += z["passes"]
+        warm += w["passes"]
+        warm_shared += ws["passes"]
+        g.close()
+    assert warm * 5 <= zero * 4, (warm, zero)
+    assert warm_shared * 3 <= zero, (warm_shared, zero)
 
 
 def test_waves_reach_the_gap_in_fewer_passes(ctx):
