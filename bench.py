@@ -342,7 +342,8 @@ def convergence(ctx, gap: float = 0.01, max_passes: int = 400) -> dict:
     D = runs["zero"]["density"]
     out = {"graph": {"kind": "rmat scale 16, edge factor 16, 8 planted G(n_c, 0.5), n_c in [100, 400]",
                      "n": g.n, "m": g.m}, "k": k, "gap": gap,
-           "train": {"graphs": len(train), "vertices": int(X.shape[0]), "loss": loss, "seconds": train_s}}
+           "train": {"graphs": len(train), "vertices": int(X.shape[0]), "loss": loss, "seconds": train_s},
+           "warm_t0": W.DEFAULT_T0}
     for label, r in runs.items():
         to_d = W.passes_to_density(r["trace"], D * (1 - 1e-12))
         out[label] = {"passes": r["passes"], "seconds": r["seconds"], "reached": r["reached"],
