@@ -545,20 +545,23 @@ struct Vals64 {
   }
 };
 
-// Shared loads (KCLPP_SEQ_SHARED): a vertex's current value is the root's
-// copy of the pass's one load vector (base, refreshed from it when a stream
-// starts) plus the increments the CTA's closed streams added (acc) plus this
-// stream's own (a u32 per vertex, owned by lane v & 31 as in Vals64).  Other
-// warps refresh and close concurrently, so a read is a recent snapshot: the
-// values steer which member gets a unit, never whether a unit is given.
+// Shared loads (KCLPP_SEQ_SHARED): a vertex's current value is the CTA's copy
+// of the pass's one load vector -- 32 bits, relative to the smallest value
+// of the root's vertices when the root started, capped at kSharedCap --
+// refreshed from the vector when a stream starts and raised by the CTA's
+// closing streams, plus this stream's own increments (a u32 per vertex, owned
+// by lane v & 31 as in Vals64).  Other warps refresh and close concurrently,
+// so a read is a recent snapshot, and a capped value hides how far above the
+// others it is: the values steer which member gets a unit, never whether a
+// unit is given.
+constexpr uint32_t kSharedCap = 1u << 29;
 struct ValsShared {
-  using T = unsigned long long;
-  const unsigned long long *base;
-  const unsigned long long *acc;
+  using T = uint32_t;
+  const uint32_t *cur;
   uint32_t *dl;
   __device__ __forceinline__ T get(int v, uint32_t &raw) const {
     raw = dl[v];
-    return base[v] + *(const volatile unsigned long long *)(acc + v) + raw;
+    return *(const volatile uint32_t *)(cur + v) + raw;
   }
   __device__ __forceinline__ void bump(int v, uint32_t raw, uint32_t *err) const {
     if (raw == 0xffffffffu) atomicOr(err, ERR_OVERFLOW);
@@ -807,11 +810,11 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
 
 // KCLPP_SEQ_SHARED: every root-edge stream of the current root against the
 // pass's one load vector r (updated in place).  When a stream starts, the
-// CTA's copy of its vertices' values is refreshed from r (less what the CTA
-// itself already added, which acc holds); the chain is the reference's
-// (kCDensestNoAtom.c:155-268) on base + acc + the stream's own increments;
-// when it closes, its increments go to acc (seen at once by the CTA's other
-// streams) and, by atomic adds, to r (seen by every stream that starts
+// CTA's copy of its vertices' values is raised to r's (relative to off, the
+// root's smallest value when it started); the chain is the reference's
+// (kCDensestNoAtom.c:155-268) on the copy plus the stream's own increments;
+// when it closes, its increments go to the copy (seen at once by the CTA's
+// other streams) and, by atomic adds, to r (seen by every stream that starts
 // later).  Every clique still gives exactly one unit to one of its members,
 // so r / T stays a feasible load whatever the interleaving; which member
 // gets it depends on the timing of the other streams (not deterministic).
@@ -820,16 +823,17 @@ __device__ __forceinline__ void seq_streams(uint32_t *next, int d, const uint32_
 // serialises on the few L2 slices that hold them.
 template <int K, int WPL>
 __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const uint32_t *rows, const uint32_t *list,
-                                                   uint32_t s, unsigned long long *r, unsigned long long *base,
-                                                   unsigned long long *acc, uint32_t *dl, int lane, uint32_t *err) {
-  const ValsShared va{base, acc, dl};
+                                                   uint32_t s, unsigned long long *r, unsigned long long off,
+                                                   uint32_t *cur, uint32_t *dl, int lane, uint32_t *err) {
+  const ValsShared va{cur, dl};
   auto id = [&](int i) { return i < d ? list[i] : s; };
   auto refresh = [&](int i) {
-    base[i] = __ldcg(r + id(i)) - *(volatile unsigned long long *)(acc + i);
+    const unsigned long long v = __ldcg(r + id(i)) - off;
+    atomicMax(cur + i, v < kSharedCap ? (uint32_t)v : kSharedCap);
   };
-  auto close = [&](int i, unsigned long long x) {
-    atomicAdd(acc + i, x);
-    atomicAdd(r + id(i), x);
+  auto close = [&](int i, uint32_t x) {
+    atomicAdd(cur + i, x);
+    atomicAdd(r + id(i), (unsigned long long)x);
   };
   for (;;) {
     int q = 0;
@@ -840,11 +844,10 @@ __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const 
     const Bits<WPL> C = load_row<WPL, true>(rows, j, 0, lane);
     if (!any_bits<WPL>(C)) continue;
     // Refresh the members' values and take, per word of C (lane = word), the
-    // smallest of them: values only grow while the stream runs (up to the
-    // races of concurrent refreshes, which change which member gets a unit,
-    // never whether one is given), so a word whose candidates all start at or
-    // above the prefix's reach falls to the prefix whole (the chain's skip).
-    unsigned long long lo = ~0ull;
+    // smallest of them: values only grow while the stream runs, so a word
+    // whose candidates all start at or above the prefix's reach falls to the
+    // prefix whole (the chain's skip).
+    uint32_t lo = 0xffffffffu;
 #pragma unroll
     for (int qq = 0; qq < WPL; ++qq) {
       uint32_t nz = __ballot_sync(KCL_FULL, C.w[qq] != 0);
@@ -852,28 +855,28 @@ __device__ __forceinline__ void seq_streams_shared(uint32_t *next, int d, const 
         const int L = __ffs(nz) - 1;
         nz &= nz - 1;
         const uint32_t word = __shfl_sync(KCL_FULL, C.w[qq], L);
-        unsigned long long val = ~0ull;
+        uint32_t val = 0xffffffffu;
         if ((word >> lane) & 1u) {
           const int i = ((L + 32 * qq) << 5) | lane;
           refresh(i);
           dl[i] = 0;
-          val = base[i] + *(volatile unsigned long long *)(acc + i);
+          val = *(volatile uint32_t *)(cur + i);
         }
-        val = warp_min_u64(val);
+        val = __reduce_min_sync(KCL_FULL, val);
         if (qq == 0 && lane == L) lo = val;
       }
     }
-    unsigned long long vj = 0, vd = 0;
+    uint32_t vj = 0, vd = 0;
     if (lane == 0) {
       refresh(j);
       refresh(d);
-      vj = base[j] + *(volatile unsigned long long *)(acc + j);
-      vd = base[d] + *(volatile unsigned long long *)(acc + d);
+      vj = *(volatile uint32_t *)(cur + j);
+      vd = *(volatile uint32_t *)(cur + d);
     }
     __syncwarp();
     const int g0 = __shfl_sync(KCL_FULL, vj < vd ? j : d, 0);  // kCDensestNoAtom.c:287
-    const unsigned long long c0 = __shfl_sync(KCL_FULL, vj < vd ? vj : vd, 0);
-    const unsigned long long c1 = seq_rec<K - 2, WPL, ValsShared, (WPL == 1)>(C, c0, rows, va, lo, lane, err);
+    const uint32_t c0 = __shfl_sync(KCL_FULL, vj < vd ? vj : vd, 0);
+    const uint32_t c1 = seq_rec<K - 2, WPL, ValsShared, (WPL == 1)>(C, c0, rows, va, lo, lane, err);
     for_members<WPL>(C, lane, [&](int i) {
       const uint32_t x = dl[i];
       if (x) close(i, x);
@@ -938,6 +941,7 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
   __shared__ uint32_t s_idx;
   __shared__ int s_tau;
   __shared__ unsigned long long s_sum;
+  __shared__ unsigned long long s_off;  // shared-load Seq: the root's smallest value
 
   if constexpr (MODE == MODE_SEQ) {
     for (int i = tid; i <= dmax; i += NW * 32) acc[i] = 0;
@@ -958,6 +962,7 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
         s_idx = idx;
         s_tau = 0;
         s_sum = 0;
+        s_off = ~0ull;
         if (a.active && idx != UINT32_MAX) a.active[blockIdx.x] = idx;  // visible to thieves
       }
     }
@@ -1000,9 +1005,24 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
       if (tid == 0) base[d] = vertex_key(a, s);
     }
     if constexpr (MODE == MODE_SEQ) {
-      if (a.shared_loads) {  // the load vector as it is now (from L2: other SMs add to it)
-        for (int i = tid; i < d; i += NW * 32) base[i] = __ldcg(a.out + a.cols[o + i]);
-        if (tid == 0) base[d] = __ldcg(a.out + s);
+      if (a.shared_loads) {
+        // The load vector as it is now (from L2: other SMs add to it), as 32-bit
+        // values relative to its smallest entry among the root's vertices, in
+        // the acc array (which this mode does not otherwise use).
+        uint32_t *cur = reinterpret_cast<uint32_t *>(acc);
+        unsigned long long mn = ~0ull;
+        for (int i = tid; i <= d; i += NW * 32) {
+          base[i] = __ldcg(a.out + (i < d ? a.cols[o + i] : s));
+          mn = base[i] < mn ? base[i] : mn;
+        }
+        mn = warp_min_u64(mn);
+        if (lane == 0) atomicMin(&s_off, mn);
+        __syncthreads();
+        const unsigned long long off = s_off;
+        for (int i = tid; i <= d; i += NW * 32) {
+          const unsigned long long v = base[i] - off;
+          cur[i] = v < kSharedCap ? (uint32_t)v : kSharedCap;
+        }
       } else {
         for (int i = tid; i < d; i += NW * 32) base[i] = a.r_in[a.cols[o + i]];
         if (tid == 0) base[d] = a.r_in[s];
@@ -1056,7 +1076,8 @@ __global__ void __launch_bounds__(warps_m<MODE, K>() * 32, min_ctas_m<MODE, K>()
     }
     if constexpr (MODE == MODE_SEQ) {
       if (a.shared_loads)
-        seq_streams_shared<K, WPL>(next, d, rows, list, s, a.out, base, acc, dl, lane, a.err);
+        seq_streams_shared<K, WPL>(next, d, rows, list, s, a.out, s_off, reinterpret_cast<uint32_t *>(acc), dl,
+                                   lane, a.err);
       else
         seq_streams<K, WPL>(next, d, rows, base, dl, acc, lane, a.err);
       __syncthreads();
