@@ -240,9 +240,10 @@ kclpp_status kclpp_count_cliques(kclpp_ctx *ctx, const kclpp_graph *g, int k,
  * *total (host, optional) receives the number of k-cliques.  The scheduler's
  * counters live in a static device array of fixed size, so n is limited to
  * 2,097,152 vertices and out-degrees to 1024 (KCLPP_ERR_UNSUPPORTED beyond).
- * The first call on a device looks the array's address up: make it before
- * any stream capture.  Calls share the array, so calls whose kernels overlap
- * on the GPU race; the call returns after synchronising `stream`. */
+ * The call ends by reading its status back and synchronising `stream`, so it
+ * must not be called while any stream is being captured: it returns
+ * KCLPP_ERR_INVALID when `stream` reports a capture in progress.  Calls share
+ * the array, so calls whose kernels overlap on the GPU race. */
 kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, uint64_t m, const uint64_t *offsets_dev,
                                          const uint32_t *cols_dev, int k, uint64_t *nck_dev,
                                          uint64_t *total);

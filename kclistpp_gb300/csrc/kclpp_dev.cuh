@@ -84,7 +84,7 @@ __device__ __forceinline__ void root_span(const PassArgs &a, uint32_t s, uint64_
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
-  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
 

@@ -34,7 +34,9 @@ cudaError_t launch_count(int k, const TierLaunch &t, dev::PassArgs a, cudaStream
 // uses before launching, and two calls whose kernels overlap on the GPU (for
 // instance on two streams at once) race on it.  The first call on each device
 // looks up the array's device address (cudaGetSymbolAddress, with that device
-// current); make that first call before any stream capture.
+// current).  No call may be made while a stream is being captured: the call
+// ends with a read-back of its status and a synchronisation, so it returns
+// KCLPP_ERR_INVALID when the stream reports a capture in progress.
 constexpr uint32_t kNoAllocMaxVertices = 1u << 21;
 constexpr uint32_t kNoAllocHeader = 64;  // words before the per-vertex counters
 
@@ -109,6 +111,11 @@ extern "C" kclpp_status kclpp_count_cliques_noalloc(void *stream, uint32_t n, ui
                      "kclpp_count_cliques_noalloc: %u vertices exceed its limit of %u (use kclpp_count_cliques)", n,
                      kNoAllocMaxVertices);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // The call reads its status back and synchronises, neither of which a
+  // stream capture allows: refuse instead of invalidating the capture.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return set_error(KCLPP_ERR_INVALID, "kclpp_count_cliques_noalloc: called while a stream capture is in progress");
   int device = 0, sms = 1;
   uint32_t *scr = nullptr;
   cudaError_t e = cudaGetDevice(&device);

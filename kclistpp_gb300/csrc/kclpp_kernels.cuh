@@ -588,52 +588,45 @@ __device__ __forceinline__ int distance(T av, T c) {
   }
 }
 
+// The fixed point of one 32-candidate word of the chain: lane b stands for
+// candidate b of the word (valid when its bit is set), rel its distance to
+// the prefix value c at the word's start.  Candidate i falls to the prefix
+// iff rel_i >= the number of earlier candidates of the word that fell to it
+// (kCDensestNoAtom.c:162-171 and 180-186, resolved by ballots).  Returns the
+// mask of the candidates that fall.
+__device__ __forceinline__ uint32_t word_fixed_point(int rel, uint32_t lt) {
+  // Start from "every candidate at or above c falls": once the loads have
+  // spread, that guess is already exact and one vote confirms it; ties (the
+  // first pass) take a few more rounds.  When no candidate is at or above c,
+  // every one takes its clique and the guess is the fixed point already.
+  uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
+  if (m) {
+    uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+    if (m2 != m) {
+      m = m2;
+      for (int r = 0; r < 32; ++r) {
+        m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
+        if (m2 == m) break;
+        m = m2;
+      }
+    }
+  }
+  return m;
+}
+
 // The Seq chain over V (the last level), one 32-bit word of V at a time: lane
 // b stands for candidate 32 * word + b.  c is the current value of the prefix
 // argmin (kCDensestNoAtom.c:162-171 and 180-186: each clique goes to the
 // candidate w when r[w] < c, strict, else to the prefix argmin, whose value
-// then grows by one).  Inside a word the chain is resolved by a ballot fixed
-// point: candidate i falls to the prefix iff its distance to c is >= the
-// number of earlier candidates of the word that fell to it.  Returns the
-// prefix argmin's new value.
-//
-// lo (Vals32, one word per lane): the smallest value the stream started with
-// among C's members in that lane's word of the bitmap.  Values only grow, so
-// a word of V whose candidates all start at or above c + (candidates before
-// them) falls to the prefix whole; the leading run of such words is settled
-// by one scan and skipped.
-template <int WPL, typename VA, bool SKIP>
-__device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typename VA::T c, const VA &va,
-                                                      typename VA::T lo, int lane, uint32_t *err) {
+// then grows by one).  Returns the prefix argmin's new value.
+template <int WPL, typename VA>
+__device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typename VA::T c, const VA &va, int lane,
+                                                      uint32_t *err) {
   using T = typename VA::T;
   const uint32_t lt = lanemask_lt();
-  uint32_t skip_mask = 0;
-  uint32_t nz0 = 0;  // SKIP: the nonzero words of V, computed once
-  if constexpr (SKIP && WPL == 1) {
-    nz0 = __ballot_sync(KCL_FULL, V.w[0] != 0);
-    if (!nz0) return c;
-  }
-  // The scan pays off from two words on; a single word goes straight to its
-  // own fixed point.
-  if (SKIP && WPL == 1 && (nz0 & (nz0 - 1))) {
-    const uint32_t pop = (uint32_t)__popc(V.w[0]);
-    uint32_t incl = pop;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(KCL_FULL, incl, o);
-      if (lane >= o) incl += t;
-    }
-    const bool ok = pop == 0 || lo >= c + (T)(incl - 1);
-    const uint32_t bad = __ballot_sync(KCL_FULL, !ok);
-    const int fb = bad ? __ffs(bad) - 1 : 32;
-    if (fb > 0) {
-      c += (T)__shfl_sync(KCL_FULL, incl, fb - 1);
-      skip_mask = fb == 32 ? 0xffffffffu : (1u << fb) - 1u;
-    }
-  }
 #pragma unroll
   for (int q = 0; q < WPL; ++q) {
-    uint32_t nz = (SKIP && WPL == 1) ? (nz0 & ~skip_mask) : __ballot_sync(KCL_FULL, V.w[q] != 0);
+    uint32_t nz = __ballot_sync(KCL_FULL, V.w[q] != 0);
     while (nz) {
       const int L = __ffs(nz) - 1;
       nz &= nz - 1;
@@ -643,28 +636,48 @@ __device__ __forceinline__ typename VA::T chain_words(const Bits<WPL> &V, typena
       int rel = -1;
       uint32_t raw = 0;
       if (valid) rel = distance<T>(va.get(v, raw), c);
-      // Fixed point from "every candidate at or above c falls": once the
-      // loads have spread, that guess is already exact and one vote confirms
-      // it; ties (the first pass) take a few more rounds.
-      // (When no candidate is at or above c, every one takes its clique and
-      // the guess is the fixed point already: the second vote is skipped.)
-      uint32_t m = __ballot_sync(KCL_FULL, rel >= 0);
-      if (m) {
-        uint32_t m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
-        if (m2 != m) {
-          m = m2;
-          for (int r = 0; r < 32; ++r) {
-            m2 = __ballot_sync(KCL_FULL, rel >= __popc(m & lt));
-            if (m2 == m) break;
-            m = m2;
-          }
-        }
-      }
+      const uint32_t m = word_fixed_point(rel, lt);
       if (valid && !((m >> lane) & 1u)) va.bump(v, raw, err);
       c += (T)__popc(m);
     }
   }
   return c;
+}
+
+// The same chain over V of one word per lane (lane w holds word w of V) with
+// 32-bit values, skipping the words that fall whole.  lo (lane w): the
+// smallest value the stream started with among C's members in word w.
+// Values only grow, and the prefix value at any candidate of V is at most c
+// plus the number of candidates before it (< tot), so every candidate of a
+// word with lo >= c + tot - 1 falls to the prefix: only the other words run
+// their fixed point, in order, each from its exact prefix value c + (the
+// candidates of V before it) - (those of them that took their clique).
+template <typename VA>
+__device__ __forceinline__ uint32_t chain_word1(uint32_t q, uint32_t c, const VA &va, uint32_t lo, int lane,
+                                                uint32_t *err) {
+  const uint32_t pop = (uint32_t)__popc(q);
+  const uint32_t tot = __reduce_add_sync(KCL_FULL, pop);
+  if (!tot) return c;
+  uint32_t bad = __ballot_sync(KCL_FULL, pop != 0u && lo < c + tot - 1u);
+  if (!bad) return c + tot;
+  const uint32_t lt = lanemask_lt();
+  uint32_t taken = 0;
+  do {
+    const int L = __ffs(bad) - 1;
+    bad &= bad - 1;
+    const uint32_t before = __reduce_add_sync(KCL_FULL, lane < L ? pop : 0u);
+    const uint32_t cL = c + before - taken;
+    const uint32_t word = __shfl_sync(KCL_FULL, q, L);
+    const bool valid = (word >> lane) & 1u;
+    const int v = (L << 5) | lane;
+    int rel = -1;
+    uint32_t raw = 0;
+    if (valid) rel = (int)(va.get(v, raw) - cL);
+    const uint32_t m = word_fixed_point(rel, lt);
+    if (valid && !((m >> lane) & 1u)) va.bump(v, raw, err);
+    taken += (uint32_t)(__popc(word) - __popc(m));
+  } while (bad);
+  return c + tot - taken;
 }
 
 // Current value of vertex x, read by the lane that owns it and broadcast.
@@ -679,13 +692,57 @@ __device__ __forceinline__ typename VA::T value_of(int x, const VA &va, int lane
 // Level L of a root-edge stream over candidates P with prefix argmin g of
 // current value cg (kCDensestNoAtom.c:173-188 for L = 2, 237-259 above).
 // Returns g's new value; the argmin of a deeper prefix, when it is u, is
-// written back by u's lane.
+// written back by u's lane.  SKIP (one word per lane, 32-bit values): the
+// last level runs chain_word1 with lo, the per-word lower bounds.
 template <int L, int WPL, typename VA, bool SKIP>
 __device__ __forceinline__ typename VA::T seq_rec(const Bits<WPL> &P, typename VA::T cg, const uint32_t *rows,
                                                   const VA &va, typename VA::T lo, int lane, uint32_t *err) {
   using T = typename VA::T;
   if constexpr (L == 1) {
-    return chain_words<WPL, VA, SKIP>(P, cg, va, lo, lane, err);
+    if constexpr (SKIP) {
+      static_assert(WPL == 1 && sizeof(T) == 4, "the word skip needs one word per lane and 32-bit values");
+      return chain_word1<VA>(P.w[0], cg, va, lo, lane, err);
+    } else {
+      return chain_words<WPL, VA>(P, cg, va, lane, err);
+    }
+  } else if constexpr (WPL == 1) {
+    if constexpr (L >= 3) {
+      const uint32_t pc = __reduce_add_sync(KCL_FULL, (uint32_t)__popc(P.w[0]));  // kCDensestNoAtom.c:218
+      if (pc < (uint32_t)L) return cg;
+    }
+    // The members u of P in ascending order, word a of P at a time.  Row u =
+    // 32 a + b keeps a + 1 words, packed from tri_off(32 a) = 16 a (a + 1)
+    // with a stride of a + 1 words between the rows of word a.
+    uint32_t nzw = __ballot_sync(KCL_FULL, P.w[0] != 0);
+    while (nzw) {
+      const int a = __ffs(nzw) - 1;
+      nzw &= nzw - 1;
+      uint32_t wb = __shfl_sync(KCL_FULL, P.w[0], a);
+      const uint32_t stride = (uint32_t)a + 1u;
+      const uint32_t *row0 = rows + 16u * (uint32_t)a * stride + (uint32_t)lane;
+      const bool in_row = lane <= a;
+      while (wb) {
+        const int b = __ffs(wb) - 1;
+        wb &= wb - 1;
+        const int u = (a << 5) | b;
+        // u's value: its word is written by lane b only; the warp barrier
+        // orders those writes before every lane's read.
+        __syncwarp();
+        uint32_t raw;
+        const T vu = va.get(u, raw);
+        const bool take = vu < cg;  // strict: ties stay with the earlier argmin
+        Bits<1> Q;
+        Q.w[0] = in_row ? (P.w[0] & row0[(uint32_t)b * stride]) : 0u;
+        const T c0 = take ? vu : cg;
+        const T c1 = seq_rec<L - 1, 1, VA, SKIP>(Q, c0, rows, va, lo, lane, err);
+        if (take) {
+          if (lane == b) va.add(u, c1 - c0, err);
+        } else {
+          cg = c1;
+        }
+      }
+    }
+    return cg;
   } else {
     if constexpr (L >= 3) {
       const int pc = warp_sum(popc_lane(P));  // kCDensestNoAtom.c:218

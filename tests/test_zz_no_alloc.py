@@ -57,3 +57,42 @@ def test_noalloc_rejects_sizes_beyond_its_limit():
                                             C.c_void_p(16), None)
     assert st == K.ERR_UNSUPPORTED
     assert b"limit" in K._lib.kclpp_last_error()
+
+
+def test_noalloc_refuses_a_capturing_stream():
+    """The call reads its status back and synchronises, which a capture does
+    not allow: on a stream being captured it returns KCLPP_ERR_INVALID and
+    leaves the capture intact."""
+    torch = pytest.importorskip("torch")
+    ctx = K.Context(0)
+    g = K.build_graph(ctx, K.planted(500, 6.0, 2.2, 1, 40, 40, 0.6, seed=3))
+    off, cols = g.csr()
+    d_off = torch.from_numpy(off.view(np.int64).copy()).cuda()
+    d_cols = torch.from_numpy(cols.view(np.int32).copy()).cuda()
+    d_nck = torch.zeros(g.n, dtype=torch.int64, device="cuda")
+    x = torch.zeros(4, device="cuda")
+    s = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.graph(graph, stream=s):
+        x.add_(1)
+        st = K._lib.kclpp_count_cliques_noalloc(C.c_void_p(s.cuda_stream), g.n, g.m, C.c_void_p(d_off.data_ptr()),
+                                                C.c_void_p(d_cols.data_ptr()), 4, C.c_void_p(d_nck.data_ptr()),
+                                                None)
+    assert st == K.ERR_INVALID
+    assert b"capture" in K._lib.kclpp_last_error()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert x.tolist() == [1.0] * 4
+    assert int(d_nck.abs().sum()) == 0
+    # outside the capture the same call runs
+    tot, per = K.count_cliques(g, 4)
+    total = C.c_uint64(0)
+    st = K._lib.kclpp_count_cliques_noalloc(C.c_void_p(s.cuda_stream), g.n, g.m, C.c_void_p(d_off.data_ptr()),
+                                            C.c_void_p(d_cols.data_ptr()), 4, C.c_void_p(d_nck.data_ptr()),
+                                            C.byref(total))
+    assert st == K.OK, K._lib.kclpp_last_error()
+    assert total.value == tot
+    assert np.array_equal(d_nck.cpu().numpy().view(np.uint64), per)
+    g.close()
+    ctx.close()
