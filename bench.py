@@ -464,6 +464,111 @@ def sampling_workload(K, ctx, a) -> dict:
     return out
 
 
+def large_workload(K, ctx, a) -> dict:
+    """The large configuration's shape -- Chung-Lu n = 4M, exponent 2.1,
+    average degree 50, 50 planted G(n_c, 0.5) communities -- at k = --large-k
+    (default 4) for --large-passes passes, the communities' sizes set by
+    --large-nc.  The configuration's k = 6 is beyond a run here: the Chung-Lu
+    background alone has degeneracy ~770, and its 6-clique count did not
+    finish in 25 minutes on a GB300 even with communities of 100-250.  Times
+    the core order, the count, T Seq and T Sim passes on the whole graph (on
+    device buffers), the exact k-clique core trim, and on the trimmed core T
+    Seq passes, the extraction and the certificate; checks the count, the
+    trim's core against the oracle's count and one Seq and one Sim pass on
+    the trimmed core against the oracle bit for bit."""
+    import torch
+    from oracle import oracle as O
+
+    lo_c, hi_c = (int(x) for x in a.large_nc.split(","))
+    k, T = a.large_k, a.large_passes
+    out = {"metric": METRIC, "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "u64+f64",
+           "data": "synthetic"}
+    cfg = {"workload": f"large: Chung-Lu n = 4M, exponent 2.1, average degree 50, 50 planted G(n_c, 0.5) "
+                       f"communities, n_c in [{lo_c}, {hi_c}], k = {k}, T = {T}",
+           "k": k, "passes": T}
+    t0 = time.perf_counter()
+    el = K.planted(4_000_000, 50.0, 2.1, 50, lo_c, hi_c, 0.5, seed=a.seed)
+    cfg["gen_s"] = round(time.perf_counter() - t0, 2)
+    t0 = time.perf_counter()
+    g = K.build_graph(ctx, el)
+    cfg["build_s"] = round(time.perf_counter() - t0, 2)
+    cfg.update(n=g.n, m=g.m, core=g.core)
+    print(f"large: n {g.n} m {g.m} core {g.core}, generated in {cfg['gen_s']} s, ordered in {cfg['build_s']} s",
+          file=sys.stderr, flush=True)
+    K.count_cliques(g, k)  # warm-up
+    t0 = time.perf_counter()
+    total, per = K.count_cliques(g, k)
+    count_s = time.perf_counter() - t0
+    out["count"] = {"cliques": total, "seconds": round(count_s, 3), "k_cliques_per_s": total / count_s,
+                    "per_vertex_sums_to_k_times_total": int(per.sum()) == k * total}
+    print(f"large: {total} {k}-cliques in {count_s:.2f} s", file=sys.stderr, flush=True)
+    stream = torch.cuda.current_stream()
+    r = torch.zeros(g.n, dtype=torch.int64, device="cuda")
+    rho = torch.zeros(g.n, dtype=torch.float64, device="cuda")
+    K.seq_passes_dev(g, k, 1, r.data_ptr())  # warm-up (and the first pass's ties)
+    K.sim_passes_dev(g, k, 1, 1, rho.data_ptr())
+    ctx.synchronize()
+    r.zero_()
+    rho.zero_()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev[0].record(stream)
+    K.seq_passes_dev(g, k, T, r.data_ptr())
+    ev[1].record(stream)
+    K.sim_passes_dev(g, k, 1, T, rho.data_ptr())
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    seq_ms = ev[0].elapsed_time(ev[1]) / T
+    sim_ms = ev[1].elapsed_time(ev[2]) / T
+    rh = r.cpu().numpy().view(np.uint64)
+    info, _ = K.extract_densest_seq(g, k, T, rh.copy())
+    out["value"] = 2 * total / ((seq_ms + sim_ms) / 1000.0)
+    out["ms_per_step"] = seq_ms + sim_ms
+    out["steps"] = T
+    out["passes"] = {"seq_ms": seq_ms, "sim_ms": sim_ms, "seq_k_cliques_per_s": total / (seq_ms / 1000.0),
+                     "sim_k_cliques_per_s": total / (sim_ms / 1000.0),
+                     "seq_conserves": int(rh.sum()) == T * total,
+                     "densest": {"n": info.n, "m": info.m, "cliques": info.cliques, "density": info.density,
+                                 "ub": info.ub}}
+    print(f"large: Seq {seq_ms:.1f} ms, Sim {sim_ms:.1f} ms per pass", file=sys.stderr, flush=True)
+    g.close()
+    t0 = time.perf_counter()
+    tr = K.trim(ctx, el, k, K.TRIM_EXACT)
+    trim_s = time.perf_counter() - t0
+    ti = tr.info
+    P = tr.edges.pairs()
+    out["trim"] = {"seconds": round(trim_s, 2), "k_core_vertices": ti.n2, "cliques_in_k_core": ti.total,
+                   "core_number": ti.ckcore, "density": ti.ckrho, "trimmed_vertices": ti.ntrim,
+                   "trimmed_edges": ti.mtrim, "trimmed_cliques": ti.ncktrim, "peel": tr.peel.as_dict()}
+    print(f"large: trim {trim_s:.1f} s -> {ti.ntrim} vertices, {ti.ncktrim} cliques", file=sys.stderr, flush=True)
+    gt = K.build_graph(ctx, K.EdgeList.from_pairs(P))
+    og = O.Graph(P)
+    threads = os.cpu_count() or 1
+    ct, _ = K.count_cliques(gt, k)
+    rt = K.seq_passes(gt, k, T)
+    infot, _ = K.extract_densest_seq(gt, k, T, rt)
+    want = og.seq_pass(k, rt, O.SEQ_EDGE_STREAMS, threads)
+    got = K.seq_passes(gt, k, 1, rt.copy())
+    rho_t = K.sim_passes(gt, k, 1)
+    want_sim = og.sim_pass(k, 1, np.zeros(gt.n), threads)
+    t0 = time.perf_counter()
+    cert, _ = K.certify_densest(gt, k, rt, 256)
+    cert_s = time.perf_counter() - t0
+    out["trimmed_core"] = {
+        "cliques": ct, "count_matches_oracle": ct == og.count_cliques(k)[0] == ti.ncktrim,
+        "seq_pass_matches_oracle": bool(np.array_equal(got, want)),
+        "sim_pass_matches_oracle": bool(np.array_equal(rho_t.view(np.uint64), want_sim.view(np.uint64))),
+        "densest": {"n": infot.n, "m": infot.m, "cliques": infot.cliques, "density": infot.density, "ub": infot.ub},
+        "certificate": {"certified": bool(cert.certified), "inside": bool(cert.inside),
+                        "inside_method": cert.inside_method, "outside": bool(cert.outside), "n": cert.n,
+                        "cliques": cert.cliques, "density": cert.density, "seconds": round(cert_s, 2)}}
+    gt.close()
+    out["config"] = cfg
+    out["note"] = ("value: (Seq + Sim) k-cliques per second over the whole graph, passes on device buffers; "
+                   "one step = one Seq pass + one Sim pass")
+    return out
+
+
 def parity_check(K, ctx, a, g, pairs, r_start, rho_start, t_start, el_full=None) -> dict:
     """Outside the timed region, with the oracle as the checker: one Seq pass
     (per-root-edge streams) and one Sim pass on the bench graph from the state
@@ -576,9 +681,13 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--modes", default="seq,sim")
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "batch", "sampling"],
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "batch", "sampling", "large"],
                     help="rmat: the default line (RMAT-20 trimmed core); batch: many uneven graphs x k = 3..7 "
-                         "in one captured CUDA graph; sampling: Seq-Sampling++ on the untrimmed RMAT graph")
+                         "in one captured CUDA graph; sampling: Seq-Sampling++ on the untrimmed RMAT graph; "
+                         "large: the large configuration's graph (Chung-Lu 4M, exponent 2.1, planted communities)")
+    ap.add_argument("--large-nc", default="200,2000", help="planted community sizes of --workload large")
+    ap.add_argument("--large-k", type=int, default=4)
+    ap.add_argument("--large-passes", type=int, default=10)
     ap.add_argument("--batch-graphs", type=int, default=512)
     ap.add_argument("--batch-nmax", type=float, default=1e5)
     ap.add_argument("--batch-passes", type=int, default=20)
@@ -628,9 +737,9 @@ def main() -> None:
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = K.Context(local, stream=stream.cuda_stream)
-    if a.workload in ("batch", "sampling"):
+    if a.workload in ("batch", "sampling", "large"):
         if rank == 0:
-            fn = batch_workload if a.workload == "batch" else sampling_workload
+            fn = {"batch": batch_workload, "sampling": sampling_workload, "large": large_workload}[a.workload]
             print(json.dumps(fn(K, ctx, a)), flush=True)
         ctx.close()
         if dist:
