@@ -312,35 +312,39 @@ def cpu_sample(pairs: np.ndarray, k: int, modes: list[str], seconds: float, thre
 
 
 # ---------------------------------------------------------------------------
-def convergence(ctx, gap: float = 0.01, max_passes: int = 400) -> dict:
+def convergence(ctx, gap: float = 0.01, max_passes: int = 400, scale: int = 16, train_graphs: int = 16,
+                labels: tuple = ("zero", "warm", "waves", "shared", "warm_shared")) -> dict:
     """Wall time to a certified density gap on a held-out graph: the zero-start
     Seq run (per-root-edge streams) against the learned warm start, the
     wave-ordered passes, the shared-load passes (KCLPP_SEQ_SHARED) and the
-    warm start with shared-load passes.  The network is trained here on zero-start runs of
-    seeded graphs of the same families (planted Chung-Lu and RMAT with planted
-    communities, k = 5); evaluation is on an RMAT scale-16 graph with planted
-    communities that the training never saw.  Every pass is followed by the
-    extraction (sort, PAVA pass, upper bound) that certifies the gap, inside the
-    timed region."""
+    warm start with shared-load passes.  The network is trained here on
+    zero-start runs of `train_graphs` seeded graphs of the same families
+    (planted Chung-Lu and RMAT with planted communities, k = 5, half each);
+    evaluation is on an RMAT graph of `scale` with planted communities that
+    the training never saw.  Every pass is followed by the extraction (sort,
+    PAVA pass, upper bound) that certifies the gap, inside the timed region."""
     import kclistpp_gb300 as K
     from kclistpp_gb300 import warm as W
 
     k = 5
     t0 = time.perf_counter()
-    train = [K.planted(6000 + 1000 * i, 8.0, 2.2, 3, 60, 160, 0.6, seed=100 + i) for i in range(8)]
-    train += [K.rmat_planted(13 + (i % 3), 16, 4, 60, 300, 0.5, seed=200 + i) for i in range(8)]
+    half = max(1, train_graphs // 2)
+    train = [K.planted(6000 + 1000 * (i % 8), 8.0, 2.2, 3, 60, 160, 0.6, seed=100 + i) for i in range(half)]
+    train += [K.rmat_planted(13 + (i % 3), 16, 4, 60, 300, 0.5, seed=200 + i) for i in range(train_graphs - half)]
     X, Y = W.training_set(ctx, train, k, passes=64)
     model = W.WarmModel(ctx, seed=5)
     loss = model.train(X, Y, steps=800, lr=1e-2)
     train_s = time.perf_counter() - t0
-    g = K.build_graph(ctx, K.rmat_planted(16, 16, 8, 100, 400, 0.5, seed=79))
+    comms = 8 << max(0, scale - 16)  # the held-out graph's planted communities grow with it
+    g = K.build_graph(ctx, K.rmat_planted(scale, 16, comms, 100, 400, 0.5, seed=79))
     runs = {}
     for label, kw in (("zero", {}), ("warm", {"model": model}), ("waves", {"det_mode": K.SEQ_WAVES}),
                       ("shared", {"det_mode": K.SEQ_SHARED}),
                       ("warm_shared", {"model": model, "det_mode": K.SEQ_SHARED})):
-        runs[label] = W.time_to_gap(g, k, gap, max_passes, trace=True, **kw)
+        if label in labels:
+            runs[label] = W.time_to_gap(g, k, gap, max_passes, trace=True, **kw)
     D = runs["zero"]["density"]
-    out = {"graph": {"kind": "rmat scale 16, edge factor 16, 8 planted G(n_c, 0.5), n_c in [100, 400]",
+    out = {"graph": {"kind": f"rmat scale {scale}, edge factor 16, {comms} planted G(n_c, 0.5), n_c in [100, 400]",
                      "n": g.n, "m": g.m}, "k": k, "gap": gap,
            "train": {"graphs": len(train), "vertices": int(X.shape[0]), "loss": loss, "seconds": train_s},
            "warm_t0": W.DEFAULT_T0}
@@ -462,6 +466,24 @@ def sampling_workload(K, ctx, a) -> dict:
                    "count plus the sampling pass"}
     smp.close()
     return out
+
+
+def convergence_workload(K, ctx, a) -> dict:
+    """The learned warm start's configuration towards its stated scale: the
+    time-to-gap comparison of the default line on a held-out RMAT graph of
+    --conv-scale with --conv-train training graphs (the configuration names
+    RMAT scale 22 and 2,000 training runs)."""
+    labels = tuple(x for x in a.conv_modes.split(",") if x)
+    if "zero" not in labels:
+        labels = ("zero",) + labels
+    conv = convergence(ctx, scale=a.conv_scale, train_graphs=a.conv_train, labels=labels)
+    z = conv["zero"]["seconds"]
+    best = min((lb for lb in labels if lb != "zero"), key=lambda lb: conv[lb]["seconds"], default="zero")
+    return {"metric": "time to a certified 1% density gap (k = 5)", "value": conv[best]["seconds"], "unit": "s",
+            "n_gpus": 1, "higher_is_better": False, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": f"convergence: held-out RMAT scale {a.conv_scale} with planted communities, "
+                                   f"{a.conv_train} training graphs, modes {','.join(labels)}"},
+            "best": best, "zero_seconds": z, "convergence": conv}
 
 
 def large_workload(K, ctx, a) -> dict:
@@ -681,10 +703,14 @@ def main() -> None:
     ap.add_argument("--scale", type=int, default=20)
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--modes", default="seq,sim")
-    ap.add_argument("--workload", default="rmat", choices=["rmat", "batch", "sampling", "large"],
+    ap.add_argument("--workload", default="rmat", choices=["rmat", "batch", "sampling", "large", "convergence"],
                     help="rmat: the default line (RMAT-20 trimmed core); batch: many uneven graphs x k = 3..7 "
                          "in one captured CUDA graph; sampling: Seq-Sampling++ on the untrimmed RMAT graph; "
-                         "large: the large configuration's graph (Chung-Lu 4M, exponent 2.1, planted communities)")
+                         "large: the large configuration's graph (Chung-Lu 4M, exponent 2.1, planted communities); "
+                         "convergence: the time-to-gap comparison at --conv-scale")
+    ap.add_argument("--conv-scale", type=int, default=18)
+    ap.add_argument("--conv-train", type=int, default=128)
+    ap.add_argument("--conv-modes", default="zero,warm,shared,warm_shared")
     ap.add_argument("--large-nc", default="200,2000", help="planted community sizes of --workload large")
     ap.add_argument("--large-k", type=int, default=4)
     ap.add_argument("--large-passes", type=int, default=10)
@@ -737,9 +763,10 @@ def main() -> None:
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     ctx = K.Context(local, stream=stream.cuda_stream)
-    if a.workload in ("batch", "sampling", "large"):
+    if a.workload in ("batch", "sampling", "large", "convergence"):
         if rank == 0:
-            fn = {"batch": batch_workload, "sampling": sampling_workload, "large": large_workload}[a.workload]
+            fn = {"batch": batch_workload, "sampling": sampling_workload, "large": large_workload,
+                  "convergence": convergence_workload}[a.workload]
             print(json.dumps(fn(K, ctx, a)), flush=True)
         ctx.close()
         if dist:
