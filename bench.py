@@ -164,7 +164,7 @@ def dag_stats(off: np.ndarray, cols: np.ndarray, k: int, s_max: int = 64, split1
     impl_root = 16 + 4 * deg + out_bytes_sum + 8 * (deg + 1) + 8 * (deg + 1)
     active = deg >= max(1, k - 1)
     edge_root = None
-    survey = None
+    ref_equiv = None
     if n <= 30000:
         A = np.zeros((n, n), dtype=np.float32)
         A[src, dst] = 1.0
@@ -174,7 +174,7 @@ def dag_stats(off: np.ndarray, cols: np.ndarray, k: int, s_max: int = 64, split1
         per_edge = 8 + 4 * (deg[src] + deg[dst]) + 4 * SD + 8 * (C + 2)
         edge_root = np.zeros(n, dtype=np.int64)
         np.add.at(edge_root, src, per_edge)
-        survey = int(8 * (n + 1) + per_edge.sum() + 16 * n)
+        ref_equiv = int(8 * (n + 1) + per_edge.sum() + 16 * n)
 
     def bucket(d):
         if d <= s_max:
@@ -197,7 +197,7 @@ def dag_stats(off: np.ndarray, cols: np.ndarray, k: int, s_max: int = 64, split1
             t["impl_bytes"] += int(impl_root[s])
         if edge_root is not None:
             t["bytes"] += int(edge_root[s])
-    return {"tiers": tiers, "survey_bytes_per_pass": survey, "n": n, "m": int(len(cols))}
+    return {"tiers": tiers, "ref_equiv_bytes_per_pass": ref_equiv, "n": n, "m": int(len(cols))}
 
 
 PASS_COUNTERS = os.path.join(ROOT, "profiles", "seq_sim_pass_rmat20_k4_counters.txt")
@@ -899,9 +899,9 @@ def main() -> None:
     # edge gathers of the reference's MakeSubgraph over every root edge.
     peak, peak_kind = measured_peaks()
     roofline = None
-    if pass_ms and stats["survey_bytes_per_pass"]:
+    if pass_ms and stats["ref_equiv_bytes_per_pass"]:
         md = max(pass_ms, key=pass_ms.get)
-        bpp = stats["survey_bytes_per_pass"]
+        bpp = stats["ref_equiv_bytes_per_pass"]
         achieved = bpp / (pass_ms[md] / 1000.0) / 1e9
         st = stats_seq if md == "seq" else stats
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
