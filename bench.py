@@ -203,10 +203,14 @@ def dag_stats(off: np.ndarray, cols: np.ndarray, k: int, s_max: int = 64, split1
 PASS_COUNTERS = os.path.join(ROOT, "profiles", "seq_sim_pass_rmat20_k4_counters.txt")
 
 
-def profiled(counter: str, kernel: str):
+def profiled(counter: str, kernel: str, a=None):
     """A per-pass counter of `kernel` ("seq" or "sim") on this workload, read
     from the committed ncu summary (a "<counter> <kernel> <value>" line):
-    dram_bytes_per_pass, l2_bytes_per_pass, warp_inst_per_pass."""
+    dram_bytes_per_pass, l2_bytes_per_pass, warp_inst_per_pass.  The summary
+    was measured on the default workload (RMAT scale 20, seed 1, k = 4); for
+    any other (`a`, the parsed arguments) there is no counter (None)."""
+    if a is not None and (a.scale, a.seed, a.k) != (20, 1, 4):
+        return None
     try:
         with open(PASS_COUNTERS) as f:
             for line in f:
@@ -905,7 +909,7 @@ def main() -> None:
         achieved = bpp / (pass_ms[md] / 1000.0) / 1e9
         st = stats_seq if md == "seq" else stats
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                    "traffic": profiled("dram_bytes_per_pass", md), "kernel": f"{'seq' if md == 'seq' else 'order'} pass "
+                    "traffic": profiled("dram_bytes_per_pass", md, a), "kernel": f"{'seq' if md == 'seq' else 'order'} pass "
                     f"(tier_m_kernel/tier_s_kernel, {len(st['tiers'])} concurrent root groups)",
                     "bytes_per_launch": bpp,
                     "impl_bytes_per_launch": sum(v["impl_bytes"] for v in st["tiers"].values()),
@@ -923,7 +927,7 @@ def main() -> None:
         # instruction-issue roof (152 SMs x 4 schedulers x one warp instruction
         # per cycle at the sampled SM clock) is the one to read the pass
         # against; the bytes above are the reference-equivalent work figure.
-        wi = profiled("warp_inst_per_pass", md)
+        wi = profiled("warp_inst_per_pass", md, a)
         if wi:
             mhz = (clk or {}).get("sm_mhz") or 2070.0
             sms = torch.cuda.get_device_properties(local).multi_processor_count
@@ -931,8 +935,8 @@ def main() -> None:
             iach = wi / (pass_ms[md] / 1000.0)
             roofline["issue"] = {"bound": "issue", "achieved": iach, "peak": ipeak, "unit": "warp inst/s",
                                  "frac": iach / ipeak, "warp_inst_per_pass": wi, "sm_mhz": mhz, "sms": sms,
-                                 "l2_bytes_per_pass": profiled("l2_bytes_per_pass", md),
-                                 "dram_bytes_per_pass": profiled("dram_bytes_per_pass", md),
+                                 "l2_bytes_per_pass": profiled("l2_bytes_per_pass", md, a),
+                                 "dram_bytes_per_pass": profiled("dram_bytes_per_pass", md, a),
                                  "source": os.path.relpath(PASS_COUNTERS, ROOT)}
     kernels = [{**p, "avg_ms": p["ms"] / max(1, p["launches"])} for p in prof]
 
