@@ -194,7 +194,7 @@ def test_bench_byte_model_matches_brute_force():
             C = Ns & set(cols[off[t]:off[t + 1]].tolist())
             want += 8 + 4 * (deg[s] + deg[t]) + 4 * sum(deg[x] for x in C) + 8 * (len(C) + 2)
     st = bench.dag_stats(off.astype(np.uint64), cols.astype(np.uint32), 4)
-    assert st["survey_bytes_per_pass"] == want
+    assert st["ref_equiv_bytes_per_pass"] == want
     # the per-tier figures partition the per-root-edge part
     assert sum(v["bytes"] for v in st["tiers"].values()) == want - 8 * (n + 1) - 16 * n
 
